@@ -1,0 +1,373 @@
+#!/usr/bin/env python
+"""Key Gbit/s of the privacy-amplification hot path on GB300.
+
+Workload (the reference's default size): n = 2^27 key/seed bits, h = 83,886,080, v = 50,331,648,
+static seed with cached FP32 spectrum, do_xor_key_rest + do_compress, i.i.d. Bernoulli(0.5) bits
+from a fixed PCG64 seed.  One step = one block.  Metric: key Gbit/s = n / time per block, the
+reference's definition (PrivacyAmplification.cu:1213, 2081).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* value  -- device-timed (CUDA events on the engine's stream) K blocks with inputs resident in HBM
+            (pa_process_device), working set 1 GiB per block, so every step streams from HBM.
+* e2e    -- the same K blocks through pa_process with pinned host buffers: per block the H2D copy of
+            key_start and key_rest, the kernels, and the D2H copy of the v/8 output bytes.
+* roofline -- the dominant kernel's algorithmic bytes per launch / its mean CUDA-event duration in
+            the timed region, against MEASURED_PEAKS.json's hbm_gbs.
+* cpu_baseline -- the exact NTT convolution of the oracle on all host cores, one whole block.
+* --impl reference -- the reference has no CPU implementation of the path and its CUDA build cannot
+            run here (its sources are not on the GPU host), so this arm times the CPU port of the
+            GF(2) Toeplitz product (oracle, direct bit-packed rows) with all host threads on the same
+            workload: per step a row sample of a block, extrapolated to all v rows.
+
+For N > 1 (torchrun) every rank runs an independent replica on its own GPU (blocks are independent;
+no collective on the data path); value = all blocks of all ranks / max over ranks of the time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_BITS = 1 << 27
+V_BITS = 50331648
+H_BITS = N_BITS - V_BITS
+METRIC = "key Gbit/s"
+UNIT = "Gbit/s"
+DATA = "synthetic: i.i.d. Bernoulli(0.5) seed and key bits, PCG64 seed 0x5EED"
+WORKLOAD = ("n=2^27 (h=83886080, v=50331648), static seed with cached FP32 spectrum, do_xor_key_rest, "
+            "do_compress; one block per step")
+KEY_BUFFERS = 4  # distinct keys cycled through the timed blocks
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_inputs(nkeys):
+    from oracle.oracle import random_block  # input generator only (seeded PRNG)
+    import numpy as np
+    import privacyamplification_gb300 as pa
+    seed, _ = random_block(N_BITS, V_BITS, 0x5EED)
+    keys = []
+    for i in range(nkeys):
+        _, recv = random_block(N_BITS, V_BITS, 0x5EED + 1 + i)
+        keys.append(pa.key_split(recv, N_BITS, V_BITS))
+    return seed, keys
+
+
+def cpu_sample(seconds, cores, seed_no=0x5EED):
+    """Direct bit-packed oracle on a row sample of the bench block.  Returns (block seconds
+    extrapolated to all v rows, sample description): per-block setup (seed reversal, key packing)
+    once, plus v times the measured per-row cost."""
+    from oracle import oracle as O
+    seed, recv = O.random_block(N_BITS, V_BITS, seed_no)
+    ks, _ = O.key_split(recv, N_BITS, V_BITS)
+    t = time.perf_counter()
+    blk = O.DirectBlock(seed, ks, N_BITS, V_BITS)
+    setup = time.perf_counter() - t
+    t = time.perf_counter()
+    blk.rows(0, 512, threads=cores)
+    per_row = (time.perf_counter() - t) / 512
+    rows = int(max(512, min(V_BITS, seconds / max(per_row, 1e-9)))) // 64 * 64
+    t = time.perf_counter()
+    blk.rows(0, rows, threads=cores)
+    t_rows = time.perf_counter() - t
+    blk.close()
+    block_s = setup + V_BITS * (t_rows / rows)
+    sample = ("%d of %d output rows of the n=2^27 block in %.2f s on %d threads, plus the per-block setup "
+              "(%.2f s), extrapolated linearly to all rows" % (rows, V_BITS, t_rows, cores, setup))
+    return block_s, sample
+
+
+def cpu_baseline(threads=0):
+    """The fastest CPU restatement in the repo: one whole n=2^27 block by the exact NTT convolution
+    (oracle/pa_oracle.c, OpenMP over butterflies), timed once."""
+    from oracle import oracle as O
+    cores = threads or os.cpu_count() or 1
+    seed, recv = O.random_block(N_BITS, V_BITS, 0x5EED)
+    ks, kr = O.key_split(recv, N_BITS, V_BITS)
+    t = time.perf_counter()
+    O.ntt(seed, ks, kr, N_BITS, V_BITS, threads=cores)
+    dt = time.perf_counter() - t
+    sample = "one whole n=2^27 block (exact NTT convolution mod 2^64-2^32+1) in %.1f s on %d threads" % (dt, cores)
+    return N_BITS / dt / 1e9, cores, sample
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    # each step: one bounded sample (per-block setup + a row sample) of a fresh block, extrapolated
+    per_step = max(0.5, min(3.0, 120.0 / max(1, args.steps + args.warmup)))
+    for i in range(args.warmup):
+        cpu_sample(per_step, cores, 0x5EED + i)
+    results = [cpu_sample(per_step, cores, 0x5EED + 100 + i) for i in range(args.steps)]
+    block_s = statistics.mean(r[0] for r in results)
+    value = N_BITS / block_s / 1e9
+    sample = "per step: " + results[-1][1]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": block_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u1", "data": DATA,
+        "config": {"workload": WORKLOAD, "n": N_BITS, "h": H_BITS, "v": V_BITS,
+                   "implementation": "CPU port of the reference's GF(2) Toeplitz product (oracle/pa_oracle.c, "
+                                     "direct bit-packed rows); the reference itself has no CPU path"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import privacyamplification_gb300 as pa
+    from privacyamplification_gb300 import build as pa_build
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+    torch.cuda.set_device(local)
+    pa_build.build()
+    dev = torch.device("cuda", local)
+
+    seed, keys = make_inputs(KEY_BUFFERS)
+    eng = pa.Engine(max_sample_size=N_BITS, device_id=local)
+    eng.set_seed(seed, N_BITS, -1)
+
+    # ---------------------------------------------------------------- device-resident timed region
+    d_keys = [(torch.from_numpy(ks.view(np.int32)).to(dev), torch.from_numpy(kr.view(np.int32)).to(dev))
+              for ks, kr in keys]
+    nbytes_out = pa.output_bytes(N_BITS, V_BITS)
+    d_out = torch.empty((nbytes_out + 3) // 4, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def block(i):
+        ks, kr = d_keys[i % len(d_keys)]
+        eng.process_device(ks.data_ptr(), kr.data_ptr(), N_BITS, V_BITS, d_out.data_ptr(), stream=sh)
+
+    for i in range(args.warmup):
+        block(i)
+    eng.sync()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    eng.set_timing(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for i in range(args.steps):
+                block(i)
+            ev1.record(stream)
+        ev1.synchronize()
+        # keep the sampler alive for a short tail so that very short runs still get a sample
+        if args.steps * 1.0 < 200:
+            time.sleep(0.25)
+    torch.cuda.synchronize()
+    stats = eng.sync()
+    stage_ms, stage_blocks = eng.stage_times()
+    eng.set_timing(False)
+    t_dev = ev0.elapsed_time(ev1) / 1e3
+    if dist:
+        t = torch.tensor([t_dev], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_dev = float(t.item())
+        dist.barrier()
+
+    # ---------------------------------------------------------------- e2e through the C ABI
+    pin_keys = []
+    for ks, kr in keys:
+        pk = torch.from_numpy(ks.view(np.int32)).pin_memory().numpy().view(np.uint32)
+        pr = torch.from_numpy(kr.view(np.int32)).pin_memory().numpy().view(np.uint32)
+        pin_keys.append((pk, pr))
+    pin_out = torch.empty(nbytes_out, dtype=torch.uint8).pin_memory().numpy()
+    for i in range(args.warmup):
+        ks, kr = pin_keys[i % len(pin_keys)]
+        eng.process(ks, kr, N_BITS, V_BITS, out=pin_out)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        ks, kr = pin_keys[i % len(pin_keys)]
+        eng.process(ks, kr, N_BITS, V_BITS, out=pin_out)
+    t_e2e = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    h2d = (H_BITS // 32 + 1) * 4 + (V_BITS // 32) * 4
+    d2h = nbytes_out
+
+    if rank != 0:
+        eng.close()
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    # ---------------------------------------------------------------- roofline of the dominant kernel
+    names = ["pass_a", "pass_b", "pass_c", "finish"]
+    n = N_BITS
+    # algorithmic bytes per launch ("Kernels"): the minimum HBM traffic of each pass
+    algo = {
+        "pass_a": 4 * n + (H_BITS + 1) // 8,        # key bits in, Y (n/2 complex64) out
+        "pass_b": 12 * n,                           # Y in, seed spectrum in, Y out
+        "pass_c": 4 * n + n // 8,                   # Y in, two parity planes out
+        "finish": n // 8 + V_BITS // 8 * 2,         # planes in, key_rest in, output out
+    }
+    kern = {names[i]: stage_ms[i] for i in range(min(len(stage_ms), len(names)))}
+    top = max(kern, key=kern.get) if kern else None
+    peak, peak_kind = peaks()
+    roof = None
+    if top:
+        achieved = algo[top] / (kern[top] / 1e3) / 1e9
+        tr = traffic_from_profiles(top)
+        roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": tr, "algorithmic_bytes": algo[top],
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "fallback 6.8 TB/s"}
+    block_bytes = 20 * n + ((H_BITS + 1) + 2 * V_BITS) // 8
+    total_s = sum(stage_ms) / 1e3 if stage_ms else None
+
+    if args.no_cpu:
+        cpu = None
+    else:
+        cb, cores, sample = cpu_baseline()
+        cpu = {"value": cb, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    value = world * args.steps * N_BITS / t_dev / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
+        "config": {"workload": WORKLOAD, "n": N_BITS, "h": H_BITS, "v": V_BITS, "blocks_per_step": 1,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2: 512 MiB work array + 512 MiB seed spectrum per block"},
+        "e2e": {"value": world * args.steps * N_BITS / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps * pa.kernels_per_block(N_BITS, V_BITS),
+        "kernels_ms": kern, "kernel_blocks_timed": stage_blocks,
+        "block_hbm_model": {"bytes": block_bytes, "GB_per_s_at_kernel_sum": block_bytes / total_s / 1e9
+                            if total_s else None},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "max_residual": stats.max_residual,
+    }
+    print(json.dumps(line))
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

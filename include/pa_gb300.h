@@ -1,0 +1,121 @@
+/*
+ * pa_gb300.h -- C ABI of the GB300 privacy-amplification engine (libpa_gb300.so).
+ *
+ * Drop-in for the per-block GPU body of nicoboss/PrivacyAmplification's host loop
+ * (PrivacyAmplification/PrivacyAmplification.cu:1686-2118, `mainloop`): the launch sequence
+ * binInt2float -> calculateCorrectionFloat -> cufftExecR2C -> setFirstElementToZero ->
+ * ElementWiseProduct -> cufftExecC2R -> ToBinaryArray[NoXOR] becomes one call.  The reference has no
+ * FFI of its own; every entry point below names the reference code it replaces.
+ *
+ * Conventions (identical to the reference):
+ *   - n ("sample_size", PrivacyAmplification.cu:1248) is the block size in bits; v ("vertical_len")
+ *     the output length; h = n - v.  n and v are multiples of 32, 0 < v < n.
+ *   - Bit i of an input word array is (word[i/32] >> (31 - i%32)) & 1 (PrivacyAmplification.cu:223-257).
+ *   - key_start holds key bits 0..h (h+1 bits; bits past h are ignored), key_rest v bits: the split of
+ *     PrivacyAmplification.cu:861-892 (pa_key_split below).
+ *   - Output bit i goes to byte i/8, bit 7 - i%8 (AMPOUT_REVERSE_ENDIAN, PrivacyAmplification.h:38);
+ *     length pa_output_bytes(): v/8 bytes, or n/16 bytes when PA_FLAG_COMPRESS is clear
+ *     (PrivacyAmplification.cu:1197).
+ *   - Result: out[i] = (sum_{j=0..h} key_start[j] * seed[(i-j) mod n] mod 2) XOR key_rest[i].
+ *
+ * All functions return 0 (PA_OK) or a negative PA_ERR_* code; nothing exits the process.
+ * An engine is bound to one CUDA device and must be used from one host thread at a time.
+ */
+#ifndef PA_GB300_H
+#define PA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PA_API __attribute__((visibility("default")))
+#else
+#define PA_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PA_OK 0
+#define PA_ERR_INVALID_ARG (-1)   /* sizes / pointers rejected before any GPU work */
+#define PA_ERR_CUDA (-2)          /* a CUDA call failed; see pa_last_cuda_error() */
+#define PA_ERR_NO_SEED (-3)       /* no seed set, or its reuse_seed_amount is used up */
+#define PA_ERR_TOO_LARGE (-4)     /* n above the engine's max_sample_size */
+#define PA_ERR_PRECISION (-5)     /* FP32 residual above the limit (result withheld) */
+
+#define PA_FLAG_XOR_KEY_REST 1u   /* do_xor_key_rest (config.yaml, key-server message) */
+#define PA_FLAG_COMPRESS 2u       /* do_compress */
+
+typedef struct pa_engine pa_engine;
+
+/* Engine configuration; mirrors the config.yaml keys the hot path reads
+ * (PrivacyAmplification.cu:1244-1271). */
+typedef struct pa_config {
+    int32_t device_id;              /* gpu_device_id_to_use */
+    uint32_t max_sample_size;       /* largest n the engine will see (2^factor_exp); sizes HBM buffers */
+    uint32_t reduction_exp;         /* accepted for compatibility: power-of-two scalings cancel exactly */
+    uint32_t pre_mul_reduction_exp; /* accepted for compatibility */
+    float residual_limit;           /* precision guard: max |x - rint(x)| allowed (0 -> 0.25) */
+} pa_config;
+
+typedef struct pa_stats {
+    float max_residual;       /* largest distance of an output value to the nearest integer */
+    uint64_t popcount_key;    /* Hamming weight of key_start (count_one_of_global_key) */
+    uint64_t popcount_seed;   /* Hamming weight of the seed (count_one_of_global_seed) */
+    float gpu_ms;             /* device time of the block (CUDA events) */
+    int32_t seed_uses_left;   /* remaining blocks for the cached seed, -1 = unlimited */
+} pa_stats;
+
+/* Creates an engine on cfg->device_id and allocates its HBM working set for n <= max_sample_size.
+ * Replaces the allocation part of main() (PrivacyAmplification.cu:1536-1606). */
+PA_API int pa_create(const pa_config* cfg, pa_engine** out);
+PA_API void pa_destroy(pa_engine* e);
+
+/* Sets the Toeplitz seed (n/32 words) and computes its cached FP32 spectrum.  reuse_seed_amount
+ * follows the reference: 0 = this block only, k > 0 = the next k blocks, -1 = forever
+ * (PrivacyAmplification.cu:1786, 2099-2101).  Replaces binInt2float(seed) + cufftExecR2C(seed)
+ * (PrivacyAmplification.cu:1831, 1903). */
+PA_API int pa_set_seed(pa_engine* e, const uint32_t* seed_words, uint32_t n, int32_t reuse_seed_amount);
+
+/* Processes one block synchronously (host buffers, pageable or pinned).  key_rest may be NULL when
+ * PA_FLAG_XOR_KEY_REST is clear.  out receives pa_output_bytes(n, v, flags) bytes.  stats may be NULL.
+ * Replaces the mainloop body PrivacyAmplification.cu:1797-2042. */
+PA_API int pa_process(pa_engine* e, const uint32_t* key_start, const uint32_t* key_rest, uint32_t n, uint32_t v,
+               uint32_t flags, uint8_t* out, pa_stats* stats);
+
+/* Device-resident forms: pointers are device memory, work is queued on `stream` (a cudaStream_t;
+ * NULL = the engine's stream) and the call returns without synchronising.  d_out receives
+ * pa_output_bytes() bytes rounded up to a multiple of 4.  pa_sync() waits and fills stats. */
+PA_API int pa_set_seed_device(pa_engine* e, const uint32_t* d_seed_words, uint32_t n, int32_t reuse_seed_amount,
+                       void* stream);
+PA_API int pa_process_device(pa_engine* e, const uint32_t* d_key_start, const uint32_t* d_key_rest, uint32_t n,
+                      uint32_t v, uint32_t flags, uint8_t* d_out, void* stream);
+PA_API int pa_sync(pa_engine* e, pa_stats* stats);
+
+/* key2StartRest (PrivacyAmplification.cu:861-892), host only: recv_key has n/32+1 words; key_start
+ * receives n/32 words (zero past word h/32), key_rest v/32 words. */
+PA_API int pa_key_split(const uint32_t* recv_key, uint32_t n, uint32_t v, uint32_t* key_start, uint32_t* key_rest);
+
+/* Output length in bytes (PrivacyAmplification.cu:1197). */
+PA_API size_t pa_output_bytes(uint32_t n, uint32_t v, uint32_t flags);
+
+/* Number of kernels one pa_process_device launches for (n, v). */
+PA_API int pa_kernels_per_block(uint32_t n, uint32_t v, uint32_t flags);
+
+/* Per-kernel timing, the counterpart of the reference's STOPWATCH stage deltas
+ * (PrivacyAmplification.cu:146-166, 2053-2074).  When enabled, every block records CUDA events on its
+ * stream before the first and after each kernel (no host synchronisation).  pa_stage_times() waits
+ * for the recorded blocks and writes the mean device time per kernel in ms (up to max_stages values,
+ * order: pass A, pass B, pass C, finish; one value for single-CTA blocks), the stage count and the
+ * number of blocks averaged, then clears the record. */
+PA_API int pa_set_timing(pa_engine* e, int enable);
+PA_API int pa_stage_times(pa_engine* e, float* ms, int max_stages, int* nstages, int* nblocks);
+
+PA_API const char* pa_error_string(int code);
+PA_API int pa_last_cuda_error(pa_engine* e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PA_GB300_H */

@@ -1,0 +1,225 @@
+"""GB300 privacy-amplification engine: Python binding of the C ABI in include/pa_gb300.h.
+
+The compute path is libpa_gb300.so (hand-written sm_103a kernels, built in-tree by
+``privacyamplification_gb300.build``).  There is no CPU fallback: if the library is missing or cannot
+be loaded, every entry point raises.
+
+Typical use (the per-block body of the reference host loop, PrivacyAmplification.cu:1686-2118)::
+
+    eng = Engine(max_sample_size=1 << 27)
+    eng.set_seed(seed_words, n, reuse_seed_amount=-1)
+    key_start, key_rest = key_split(recv_key, n, v)
+    out = eng.process(key_start, key_rest, n, v)          # v/8 bytes, reference byte order
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpa_gb300.so")
+
+PA_OK = 0
+PA_ERR_INVALID_ARG = -1
+PA_ERR_CUDA = -2
+PA_ERR_NO_SEED = -3
+PA_ERR_TOO_LARGE = -4
+PA_ERR_PRECISION = -5
+FLAG_XOR_KEY_REST = 1
+FLAG_COMPRESS = 2
+DEFAULT_FLAGS = FLAG_XOR_KEY_REST | FLAG_COMPRESS
+
+# Every symbol include/pa_gb300.h declares.
+EXPORTS = ("pa_create", "pa_destroy", "pa_set_seed", "pa_process", "pa_set_seed_device", "pa_process_device",
+           "pa_sync", "pa_key_split", "pa_output_bytes", "pa_kernels_per_block", "pa_set_timing",
+           "pa_stage_times", "pa_error_string", "pa_last_cuda_error")
+
+
+class PAError(RuntimeError):
+    def __init__(self, code: int, what: str, cuda: int = 0):
+        msg = "%s failed: %s (%d)" % (what, error_string(code), code)
+        if cuda:
+            msg += ", cudaError %d" % cuda
+        super().__init__(msg)
+        self.code = code
+        self.cuda = cuda
+
+
+class PAConfig(ctypes.Structure):
+    _fields_ = [("device_id", ctypes.c_int32), ("max_sample_size", ctypes.c_uint32),
+                ("reduction_exp", ctypes.c_uint32), ("pre_mul_reduction_exp", ctypes.c_uint32),
+                ("residual_limit", ctypes.c_float)]
+
+
+class PAStats(ctypes.Structure):
+    _fields_ = [("max_residual", ctypes.c_float), ("popcount_key", ctypes.c_uint64),
+                ("popcount_seed", ctypes.c_uint64), ("gpu_ms", ctypes.c_float),
+                ("seed_uses_left", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads libpa_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("%s not found: build it with `python -m privacyamplification_gb300.build`" % path)
+    lib = ctypes.CDLL(path)
+    u32p, u8p, vp = ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint8), ctypes.c_void_p
+    eng = ctypes.c_void_p
+    sig = {
+        "pa_create": ([ctypes.POINTER(PAConfig), ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+        "pa_destroy": ([eng], None),
+        "pa_set_seed": ([eng, u32p, ctypes.c_uint32, ctypes.c_int32], ctypes.c_int),
+        "pa_process": ([eng, u32p, u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, u8p,
+                        ctypes.POINTER(PAStats)], ctypes.c_int),
+        "pa_set_seed_device": ([eng, vp, ctypes.c_uint32, ctypes.c_int32, vp], ctypes.c_int),
+        "pa_process_device": ([eng, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp],
+                              ctypes.c_int),
+        "pa_sync": ([eng, ctypes.POINTER(PAStats)], ctypes.c_int),
+        "pa_key_split": ([u32p, ctypes.c_uint32, ctypes.c_uint32, u32p, u32p], ctypes.c_int),
+        "pa_output_bytes": ([ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_size_t),
+        "pa_kernels_per_block": ([ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+        "pa_set_timing": ([eng, ctypes.c_int], ctypes.c_int),
+        "pa_stage_times": ([eng, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                            ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "pa_error_string": ([ctypes.c_int], ctypes.c_char_p),
+        "pa_last_cuda_error": ([eng], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def error_string(code: int) -> str:
+    return load_library().pa_error_string(code).decode()
+
+
+def output_bytes(n: int, v: int, flags: int = DEFAULT_FLAGS) -> int:
+    return int(load_library().pa_output_bytes(n, v, flags))
+
+
+def kernels_per_block(n: int, v: int, flags: int = DEFAULT_FLAGS) -> int:
+    return int(load_library().pa_kernels_per_block(n, v, flags))
+
+
+def _u32(a) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    return a
+
+
+def _p32(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+def key_split(recv_key, n: int, v: int):
+    """key2StartRest (PrivacyAmplification.cu:861-892) through the C ABI.
+    Returns (key_start[n/32], key_rest[v/32])."""
+    rk = _u32(recv_key)
+    if rk.size < n // 32 + 1:
+        raise ValueError("recv_key needs n/32+1 words")
+    ks = np.zeros(n // 32, np.uint32)
+    kr = np.zeros(v // 32, np.uint32)
+    rc = load_library().pa_key_split(_p32(rk), n, v, _p32(ks), _p32(kr))
+    if rc:
+        raise PAError(rc, "pa_key_split")
+    return ks, kr
+
+
+class Engine:
+    """One GPU's privacy-amplification engine (pa_create / pa_destroy)."""
+
+    def __init__(self, max_sample_size: int, device_id: int = 0, residual_limit: float = 0.25,
+                 reduction_exp: int = 11, pre_mul_reduction_exp: int = 5):
+        self._lib = load_library()
+        cfg = PAConfig(device_id, max_sample_size, reduction_exp, pre_mul_reduction_exp, residual_limit)
+        h = ctypes.c_void_p()
+        rc = self._lib.pa_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc:
+            raise PAError(rc, "pa_create")
+        self._h = h
+        self.max_sample_size = max_sample_size
+        self.last_stats = PAStats()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pa_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc:
+            raise PAError(rc, what, self._lib.pa_last_cuda_error(self._h))
+
+    def set_seed(self, seed_words, n: int, reuse_seed_amount: int = -1):
+        s = _u32(seed_words)
+        if s.size < n // 32:
+            raise ValueError("seed needs n/32 words")
+        self._check(self._lib.pa_set_seed(self._h, _p32(s), n, reuse_seed_amount), "pa_set_seed")
+
+    def process(self, key_start, key_rest, n: int, v: int, flags: int = DEFAULT_FLAGS,
+                check: bool = True, out: np.ndarray = None) -> np.ndarray:
+        ks = _u32(key_start)
+        if ks.size < (n - v) // 32 + 1:
+            raise ValueError("key_start needs h/32+1 words")
+        kr = _u32(key_rest) if key_rest is not None else None
+        if flags & FLAG_XOR_KEY_REST and (kr is None or kr.size < v // 32):
+            raise ValueError("key_rest needs v/32 words")
+        nb = output_bytes(n, v, flags)
+        if out is None:
+            out = np.zeros(nb, np.uint8)
+        elif out.dtype != np.uint8 or out.size < nb or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous uint8 array of %d bytes" % nb)
+        rc = self._lib.pa_process(self._h, _p32(ks), _p32(kr) if kr is not None else None, n, v, flags,
+                                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), ctypes.byref(self.last_stats))
+        if check or rc != PA_ERR_PRECISION:
+            self._check(rc, "pa_process")
+        return out
+
+    # ---- device-resident forms (pointers are integers, e.g. torch.Tensor.data_ptr()) -------------
+    def set_seed_device(self, d_seed: int, n: int, reuse_seed_amount: int = -1, stream: int = 0):
+        self._check(self._lib.pa_set_seed_device(self._h, d_seed, n, reuse_seed_amount, stream or None),
+                    "pa_set_seed_device")
+
+    def process_device(self, d_key_start: int, d_key_rest: int, n: int, v: int, d_out: int,
+                       flags: int = DEFAULT_FLAGS, stream: int = 0):
+        self._check(self._lib.pa_process_device(self._h, d_key_start, d_key_rest or None, n, v, flags, d_out,
+                                                stream or None), "pa_process_device")
+
+    def set_timing(self, enable: bool = True):
+        self._check(self._lib.pa_set_timing(self._h, int(enable)), "pa_set_timing")
+
+    def stage_times(self):
+        """Mean device ms per kernel over the blocks recorded since the last call, and the block count."""
+        ms = (ctypes.c_float * 8)()
+        ns, nb = ctypes.c_int(), ctypes.c_int()
+        self._check(self._lib.pa_stage_times(self._h, ms, 8, ctypes.byref(ns), ctypes.byref(nb)), "pa_stage_times")
+        return [ms[i] for i in range(ns.value)], nb.value
+
+    def sync(self, check: bool = True) -> PAStats:
+        rc = self._lib.pa_sync(self._h, ctypes.byref(self.last_stats))
+        if check or rc != PA_ERR_PRECISION:
+            self._check(rc, "pa_sync")
+        return self.last_stats

@@ -1,0 +1,423 @@
+// pa_engine.cu -- host side of the C ABI declared in include/pa_gb300.h.
+//
+// Owns the HBM working set of one GPU (the reference's device buffers di1/di2/do1/do2 and its cuFFT
+// plans, PrivacyAmplification.cu:1567-1593, 1714-1751), the cached seed spectrum and the
+// reuse_seed_amount bookkeeping of the host loop (PrivacyAmplification.cu:1762-1797, 2099-2101).
+#include "../../include/pa_gb300.h"
+#include "pa_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+using pa::BlockGeom;
+
+struct pa_engine {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t max_n = 0;
+    int cap_log_np = 0;  // largest cyclic length the buffers hold
+    float residual_limit = 0.25f;
+    // HBM working set
+    uint32_t* d_key_start = nullptr;
+    uint32_t* d_key_rest = nullptr;
+    uint32_t* d_seed = nullptr;
+    uint32_t* d_out = nullptr;
+    float2* d_work = nullptr;
+    float2* d_spec = nullptr;
+    uint32_t* d_planes = nullptr;
+    unsigned long long* d_cnt = nullptr;  // [0] key popcount, [1] seed popcount
+    unsigned int* d_resid = nullptr;
+    float2* d_glo = nullptr;
+    float2* d_ghi = nullptr;
+    int tw_log_n = -1;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // seed state
+    bool seed_valid = false;
+    uint32_t seed_n = 0;
+    int64_t seed_left = 0;  // -1 = unlimited
+    bool spec_valid = false;
+    BlockGeom spec_geom{};
+    int last_cuda = 0;
+    bool pending = false;  // device-form work queued and not yet synchronised
+    // per-kernel timing ring (pa_set_timing / pa_stage_times)
+    bool timing = false;
+    std::vector<std::array<cudaEvent_t, 5>> tev;
+    std::vector<int> tev_stages;
+    size_t tev_next = 0, tev_count = 0;
+};
+
+namespace {
+
+int ceil_log2(uint64_t x) {
+    int l = 0;
+    while ((1ull << l) < x) ++l;
+    return l;
+}
+
+bool is_pow2(uint32_t x) { return x && !(x & (x - 1u)); }
+
+int cuda_fail(pa_engine* e, cudaError_t err) {
+    e->last_cuda = (int)err;
+    return PA_ERR_CUDA;
+}
+
+#define PA_CUDA(e, call)                                  \
+    do {                                                  \
+        cudaError_t err__ = (call);                       \
+        if (err__ != cudaSuccess) return cuda_fail(e, err__); \
+    } while (0)
+
+// Block geometry (sizes, padded cyclic length, three-pass split) for (n, v, flags).
+int make_geom(uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
+    if (n < 1024u || (n & 31u) || (v & 31u) || v == 0 || v >= n) return PA_ERR_INVALID_ARG;
+    g->n = n;
+    g->v = v;
+    g->h = n - v;
+    g->out_bits = (flags & PA_FLAG_COMPRESS) ? v : n / 2u;
+    if (is_pow2(n)) {
+        g->log_np = ceil_log2(n);
+        g->seed_direct = n;
+    } else {
+        uint64_t need = std::max<uint64_t>(n, (uint64_t)g->out_bits + g->h);
+        g->log_np = ceil_log2(need);
+        uint64_t np = 1ull << g->log_np;
+        g->seed_direct = (uint32_t)std::min<uint64_t>(np - g->h, n);
+    }
+    g->log_n = g->log_np - 1;
+    if (g->log_n <= 14) {
+        g->log_n1 = g->log_n2 = 0;
+    } else {
+        g->log_n2 = std::min(14, g->log_n - 6);
+        g->log_n1 = g->log_n - g->log_n2;
+    }
+    if (g->log_n1 > 12) return PA_ERR_TOO_LARGE;
+    return PA_OK;
+}
+
+bool same_seed_geom(const BlockGeom& a, const BlockGeom& b) {
+    if (a.log_np != b.log_np || a.n != b.n) return false;
+    if (is_pow2(a.n)) return true;  // placement is the identity
+    return a.seed_direct == b.seed_direct && a.h == b.h;
+}
+
+int ensure_twiddles(pa_engine* e, const BlockGeom& g, cudaStream_t s) {
+    if (g.log_n1 == 0 || e->tw_log_n == g.log_n) return PA_OK;
+    int rc = pa::launch_twiddle_tables(g, e->d_glo, e->d_ghi, s);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    e->tw_log_n = g.log_n;
+    return PA_OK;
+}
+
+int build_spectrum(pa_engine* e, const BlockGeom& g, cudaStream_t s) {
+    int rc = ensure_twiddles(e, g, s);
+    if (rc) return rc;
+    rc = pa::launch_seed_spectrum(g, e->d_seed, e->d_spec, e->d_work, e->d_cnt + 1, {e->d_glo, e->d_ghi}, s);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    e->spec_geom = g;
+    e->spec_valid = true;
+    return PA_OK;
+}
+
+int seed_common(pa_engine* e, uint32_t n, int32_t reuse, cudaStream_t s) {
+    e->seed_valid = true;
+    e->seed_n = n;
+    e->seed_left = reuse < 0 ? -1 : std::max<int64_t>(reuse, 1);
+    e->spec_valid = false;
+    if (is_pow2(n)) {  // placement does not depend on v: build the spectrum now
+        BlockGeom g;
+        int rc = make_geom(n, n / 2u, PA_FLAG_COMPRESS, &g);
+        if (rc) return rc;
+        return build_spectrum(e, g, s);
+    }
+    return PA_OK;
+}
+
+int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const BlockGeom& g, uint32_t flags,
+                 uint32_t* d_out, cudaStream_t s) {
+    if (!e->seed_valid || e->seed_left == 0) return PA_ERR_NO_SEED;
+    if (g.n != e->seed_n) return PA_ERR_INVALID_ARG;
+    if (!e->spec_valid || !same_seed_geom(e->spec_geom, g)) {
+        int rc = build_spectrum(e, g, s);
+        if (rc) return rc;
+    }
+    int rc = ensure_twiddles(e, g, s);
+    if (rc) return rc;
+    PA_CUDA(e, cudaEventRecord(e->ev0, s));
+    cudaEvent_t* sev = nullptr;
+    if (e->timing && !e->tev.empty()) {
+        size_t slot = e->tev_next;
+        sev = e->tev[slot].data();
+        e->tev_stages[slot] = pa::kernel_count_key_block(g);
+        e->tev_next = (slot + 1) % e->tev.size();
+        e->tev_count = std::min(e->tev_count + 1, e->tev.size());
+    }
+    rc = pa::launch_key_block(g, d_ks, d_kr, flags, e->d_spec, e->d_work, e->d_planes, e->d_cnt, e->d_resid, d_out,
+                              {e->d_glo, e->d_ghi}, e->num_sms, s, sev);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    PA_CUDA(e, cudaEventRecord(e->ev1, s));
+    if (e->seed_left > 0) --e->seed_left;
+    return PA_OK;
+}
+
+int read_stats(pa_engine* e, pa_stats* st, float* resid_out) {
+    unsigned long long cnt[2] = {0, 0};
+    unsigned int rb = 0;
+    PA_CUDA(e, cudaMemcpy(cnt, e->d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost));
+    PA_CUDA(e, cudaMemcpy(&rb, e->d_resid, sizeof(rb), cudaMemcpyDeviceToHost));
+    float resid;
+    std::memcpy(&resid, &rb, sizeof(resid));
+    *resid_out = resid;
+    if (st) {
+        st->max_residual = resid;
+        st->popcount_key = cnt[0];
+        st->popcount_seed = cnt[1];
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+        st->gpu_ms = ms;
+        st->seed_uses_left = e->seed_left < 0 ? -1 : (int32_t)e->seed_left;
+    }
+    return PA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t pa_output_bytes(uint32_t n, uint32_t v, uint32_t flags) {
+    return (flags & PA_FLAG_COMPRESS) ? v / 8u : n / 16u;
+}
+
+int pa_kernels_per_block(uint32_t n, uint32_t v, uint32_t flags) {
+    BlockGeom g;
+    if (make_geom(n, v, flags, &g)) return 0;
+    return pa::kernel_count_key_block(g);
+}
+
+const char* pa_error_string(int code) {
+    switch (code) {
+        case PA_OK: return "ok";
+        case PA_ERR_INVALID_ARG: return "invalid argument";
+        case PA_ERR_CUDA: return "CUDA error";
+        case PA_ERR_NO_SEED: return "no seed set or reuse_seed_amount used up";
+        case PA_ERR_TOO_LARGE: return "block larger than the engine's max_sample_size";
+        case PA_ERR_PRECISION: return "FP32 residual above the precision limit";
+        default: return "unknown error";
+    }
+}
+
+int pa_last_cuda_error(pa_engine* e) { return e ? e->last_cuda : 0; }
+
+int pa_create(const pa_config* cfg, pa_engine** out) {
+    if (!cfg || !out || cfg->max_sample_size < 1024u || (cfg->max_sample_size & 31u)) return PA_ERR_INVALID_ARG;
+    *out = nullptr;
+    pa_engine* e = new (std::nothrow) pa_engine();
+    if (!e) return PA_ERR_INVALID_ARG;
+    e->device = cfg->device_id;
+    e->max_n = cfg->max_sample_size;
+    e->residual_limit = cfg->residual_limit > 0.f ? cfg->residual_limit : 0.25f;
+    e->cap_log_np = ceil_log2(cfg->max_sample_size);
+    if (e->cap_log_np > 27) {
+        delete e;
+        return PA_ERR_TOO_LARGE;
+    }
+    auto fail = [&](cudaError_t err) {
+        int code = (int)err;
+        pa_destroy(e);
+        (void)code;
+        return PA_ERR_CUDA;
+    };
+    cudaError_t err = cudaSetDevice(e->device);
+    if (err != cudaSuccess) return fail(err);
+    cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->device);
+    if ((err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(err);
+    if ((err = cudaEventCreate(&e->ev0)) != cudaSuccess) return fail(err);
+    if ((err = cudaEventCreate(&e->ev1)) != cudaSuccess) return fail(err);
+    size_t np = 1ull << e->cap_log_np;
+    size_t words = np / 32 + 64;
+    if ((err = cudaMalloc(&e->d_key_start, words * 4)) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_key_rest, words * 4)) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_seed, words * 4)) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_out, words * 4)) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_work, (np / 2) * sizeof(float2))) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_spec, (np / 2) * sizeof(float2))) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_planes, np / 8 + 256)) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_cnt, 2 * sizeof(unsigned long long))) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_resid, sizeof(unsigned int))) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_glo, 8192 * sizeof(float2))) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_ghi, 16384 * sizeof(float2))) != cudaSuccess) return fail(err);
+    cudaMemset(e->d_cnt, 0, 2 * sizeof(unsigned long long));
+    cudaMemset(e->d_resid, 0, sizeof(unsigned int));
+    *out = e;
+    return PA_OK;
+}
+
+void pa_destroy(pa_engine* e) {
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    cudaFree(e->d_key_start);
+    cudaFree(e->d_key_rest);
+    cudaFree(e->d_seed);
+    cudaFree(e->d_out);
+    cudaFree(e->d_work);
+    cudaFree(e->d_spec);
+    cudaFree(e->d_planes);
+    cudaFree(e->d_cnt);
+    cudaFree(e->d_resid);
+    cudaFree(e->d_glo);
+    cudaFree(e->d_ghi);
+    for (auto& a : e->tev)
+        for (auto ev : a) cudaEventDestroy(ev);
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+static int check_n(pa_engine* e, uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
+    int rc = make_geom(n, v, flags, g);
+    if (rc) return rc;
+    if (n > e->max_n || g->log_np > e->cap_log_np) return PA_ERR_TOO_LARGE;
+    return PA_OK;
+}
+
+int pa_set_seed(pa_engine* e, const uint32_t* seed_words, uint32_t n, int32_t reuse_seed_amount) {
+    if (!e || !seed_words) return PA_ERR_INVALID_ARG;
+    BlockGeom g;
+    int rc = check_n(e, n, n / 2u, PA_FLAG_COMPRESS, &g);
+    if (rc) return rc;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    PA_CUDA(e, cudaMemcpyAsync(e->d_seed, seed_words, (size_t)(n / 32u) * 4u, cudaMemcpyHostToDevice, e->stream));
+    rc = seed_common(e, n, reuse_seed_amount, e->stream);
+    if (rc) return rc;
+    PA_CUDA(e, cudaStreamSynchronize(e->stream));
+    return PA_OK;
+}
+
+int pa_set_seed_device(pa_engine* e, const uint32_t* d_seed_words, uint32_t n, int32_t reuse_seed_amount,
+                       void* stream) {
+    if (!e || !d_seed_words) return PA_ERR_INVALID_ARG;
+    BlockGeom g;
+    int rc = check_n(e, n, n / 2u, PA_FLAG_COMPRESS, &g);
+    if (rc) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    PA_CUDA(e, cudaMemcpyAsync(e->d_seed, d_seed_words, (size_t)(n / 32u) * 4u, cudaMemcpyDeviceToDevice, s));
+    e->pending = true;
+    return seed_common(e, n, reuse_seed_amount, s);
+}
+
+int pa_process(pa_engine* e, const uint32_t* key_start, const uint32_t* key_rest, uint32_t n, uint32_t v,
+               uint32_t flags, uint8_t* out, pa_stats* stats) {
+    if (!e || !key_start || !out) return PA_ERR_INVALID_ARG;
+    if ((flags & PA_FLAG_XOR_KEY_REST) && !key_rest) return PA_ERR_INVALID_ARG;
+    BlockGeom g;
+    int rc = check_n(e, n, v, flags, &g);
+    if (rc) return rc;
+    if (!e->seed_valid || e->seed_left == 0) return PA_ERR_NO_SEED;
+    if (n != e->seed_n) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    cudaStream_t s = e->stream;
+    PA_CUDA(e, cudaMemcpyAsync(e->d_key_start, key_start, (size_t)(g.h / 32u + 1u) * 4u, cudaMemcpyHostToDevice, s));
+    if (flags & PA_FLAG_XOR_KEY_REST)
+        PA_CUDA(e, cudaMemcpyAsync(e->d_key_rest, key_rest, (size_t)(v / 32u) * 4u, cudaMemcpyHostToDevice, s));
+    rc = block_common(e, e->d_key_start, e->d_key_rest, g, flags, e->d_out, s);
+    if (rc) return rc;
+    size_t ob = pa_output_bytes(n, v, flags);
+    PA_CUDA(e, cudaMemcpyAsync(out, e->d_out, ob, cudaMemcpyDeviceToHost, s));
+    PA_CUDA(e, cudaStreamSynchronize(s));
+    float resid = 0.f;
+    rc = read_stats(e, stats, &resid);
+    if (rc) return rc;
+    if (!(resid <= e->residual_limit)) {
+        std::memset(out, 0, ob);
+        return PA_ERR_PRECISION;
+    }
+    return PA_OK;
+}
+
+int pa_process_device(pa_engine* e, const uint32_t* d_key_start, const uint32_t* d_key_rest, uint32_t n, uint32_t v,
+                      uint32_t flags, uint8_t* d_out, void* stream) {
+    if (!e || !d_key_start || !d_out) return PA_ERR_INVALID_ARG;
+    if ((flags & PA_FLAG_XOR_KEY_REST) && !d_key_rest) return PA_ERR_INVALID_ARG;
+    if (reinterpret_cast<uintptr_t>(d_out) & 3u) return PA_ERR_INVALID_ARG;
+    BlockGeom g;
+    int rc = check_n(e, n, v, flags, &g);
+    if (rc) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    e->pending = true;
+    return block_common(e, d_key_start, d_key_rest, g, flags, reinterpret_cast<uint32_t*>(d_out), s);
+}
+
+int pa_sync(pa_engine* e, pa_stats* stats) {
+    if (!e) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    PA_CUDA(e, cudaDeviceSynchronize());
+    e->pending = false;
+    float resid = 0.f;
+    int rc = read_stats(e, stats, &resid);
+    if (rc) return rc;
+    return resid <= e->residual_limit ? PA_OK : PA_ERR_PRECISION;
+}
+
+int pa_set_timing(pa_engine* e, int enable) {
+    if (!e) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    if (enable && e->tev.empty()) {
+        const size_t slots = 1024;
+        e->tev.resize(slots);
+        e->tev_stages.assign(slots, 0);
+        for (auto& a : e->tev)
+            for (auto& ev : a) PA_CUDA(e, cudaEventCreate(&ev));
+    }
+    e->timing = enable != 0;
+    e->tev_next = e->tev_count = 0;
+    return PA_OK;
+}
+
+int pa_stage_times(pa_engine* e, float* ms, int max_stages, int* nstages, int* nblocks) {
+    if (!e || !ms || max_stages <= 0) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    double acc[4] = {0, 0, 0, 0};
+    int stages = 0, blocks = 0;
+    size_t n = e->tev_count, first = (e->tev_next + e->tev.size() - n) % std::max<size_t>(1, e->tev.size());
+    for (size_t k = 0; k < n; ++k) {
+        size_t slot = (first + k) % e->tev.size();
+        int st = e->tev_stages[slot];
+        if (blocks && st != stages) continue;  // average blocks of one shape only
+        stages = st;
+        PA_CUDA(e, cudaEventSynchronize(e->tev[slot][st]));
+        for (int i = 0; i < st; ++i) {
+            float t = 0.f;
+            PA_CUDA(e, cudaEventElapsedTime(&t, e->tev[slot][i], e->tev[slot][i + 1]));
+            acc[i] += t;
+        }
+        ++blocks;
+    }
+    for (int i = 0; i < std::min(stages, max_stages); ++i) ms[i] = blocks ? (float)(acc[i] / blocks) : 0.f;
+    if (nstages) *nstages = stages;
+    if (nblocks) *nblocks = blocks;
+    e->tev_next = e->tev_count = 0;
+    return PA_OK;
+}
+
+int pa_key_split(const uint32_t* recv_key, uint32_t n, uint32_t v, uint32_t* key_start, uint32_t* key_rest) {
+    if (!recv_key || !key_start || !key_rest || (n & 31u) || (v & 31u) || v == 0 || v >= n)
+        return PA_ERR_INVALID_ARG;
+    uint32_t hb = (n - v) / 32u, vb = v / 32u, nb = n / 32u;
+    std::memset(key_start, 0, (size_t)nb * 4u);
+    std::memcpy(key_start, recv_key, (size_t)hb * 4u);
+    key_start[hb] = recv_key[hb] & 0x80000000u;
+    for (uint32_t i = 0; i < vb; ++i) key_rest[i] = (recv_key[hb + i] << 1) | (recv_key[hb + i + 1] >> 31);
+    return PA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,52 @@
+// pa_kernels.cuh -- block geometry shared by the host engine and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pa {
+
+// One privacy-amplification block, sizes in bits (nicoboss/PrivacyAmplification naming:
+// sample_size n, vertical_len v, horizontal_len h; PrivacyAmplification.cu:1423-1430).
+struct BlockGeom {
+    uint32_t n, v, h;      // h = n - v
+    uint32_t out_bits;     // v (do_compress) or n/2 (PrivacyAmplification.cu:1197)
+    int log_np;            // cyclic length Np = 2^log_np >= n (== n when n is a power of two)
+    int log_n;             // complex length N = Np/2
+    int log_n1, log_n2;    // three-pass split N = N1 * N2 (0, 0 for the single-CTA path)
+    uint32_t seed_direct;  // seed positions < seed_direct map to themselves (see seed_bit)
+};
+
+// Seed placement in the cyclic length Np.  For Np == n this is the identity.  For a padded Np the
+// outputs i < out_bits see exactly the reference's seed[(i-j) mod n] when
+//   s'[x] = s[x]               for x < seed_direct = min(Np - h, n),
+//   s'[x] = s[x - (Np - n)]    for x >= Np - h,
+//   s'[x] = 0                  otherwise.
+__host__ __device__ inline int seed_source(const BlockGeom& g, uint64_t x, uint64_t* src) {
+    uint64_t np = 1ull << g.log_np;
+    if (x < g.seed_direct) { *src = x; return 1; }
+    if (x >= np - g.h) { *src = x - (np - g.n); return 1; }
+    return 0;
+}
+
+}  // namespace pa
+
+// Host launch API (pa_kernels.cu).  All launches are asynchronous on `stream`.
+namespace pa {
+struct DeviceTables {
+    const float2* glo;  // W_N^a, a < 8192
+    const float2* ghi;  // W_N^(8192 b), b < max(1, N/8192)
+};
+int launch_twiddle_tables(const BlockGeom& g, float2* glo, float2* ghi, cudaStream_t s);
+// Seed spectrum (FP32, scaled by 1/(2Np)) in the layout the key path consumes; work is scratch of
+// N complex (three-pass path only).  cnt_seed receives the popcount of the placed seed.
+int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec, float2* work,
+                         unsigned long long* cnt_seed, DeviceTables tw, cudaStream_t s);
+// Key block: out_words receives ceil(out_bits/32) little-endian words of the reference byte stream.
+// stage_ev (optional, kernel_count_key_block()+1 events) is recorded before the first kernel and
+// after each kernel.
+int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32_t* key_rest, uint32_t flags,
+                     const float2* spec, float2* work, uint32_t* planes, unsigned long long* cnt,
+                     unsigned int* resid_bits, uint32_t* out_words, DeviceTables tw, int num_sms,
+                     cudaStream_t s, cudaEvent_t* stage_ev);
+int kernel_count_key_block(const BlockGeom& g);
+}  // namespace pa

@@ -1,0 +1,65 @@
+"""The C ABI library loads and exports what include/pa_gb300.h declares; host-only entry points.
+
+No test here launches a kernel: these run on machines without a GPU.
+"""
+import os
+import re
+
+import numpy as np
+
+import privacyamplification_gb300 as pa
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "pa_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pa_[a-z_]+)\s*\(", text)))
+
+
+def test_header_matches_binding_list():
+    assert declared_functions() == sorted(pa.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(pa_lib):
+    for name in declared_functions():
+        assert hasattr(pa_lib, name), name
+
+
+def test_output_bytes():
+    assert pa.output_bytes(1 << 27, 50331648, pa.DEFAULT_FLAGS) == 50331648 // 8
+    assert pa.output_bytes(2048, 1024, 0) == 2048 // 16
+    assert pa.output_bytes(2048, 1024, pa.FLAG_XOR_KEY_REST) == 2048 // 16
+
+
+def test_kernels_per_block():
+    assert pa.kernels_per_block(2048, 1024, 0) == 1
+    assert pa.kernels_per_block(1 << 27, 50331648) == 4
+    assert pa.kernels_per_block(1000, 96) == 0  # rejected size
+
+
+def test_key_split_matches_oracle(pa_lib):
+    for n, v in [(1024, 384), (1 << 16, 24576), (4096, 4064), (4096, 32)]:
+        _, recv = O.random_block(n, v, n ^ v)
+        a = pa.key_split(recv, n, v)
+        b = O.key_split(recv, n, v)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_key_split_rejects_bad_sizes(pa_lib):
+    recv = np.zeros(1 << 10, np.uint32)
+    for n, v in [(1024, 0), (1024, 1024), (1000, 96), (1024, 100)]:
+        try:
+            pa.key_split(recv, n, v)
+        except pa.PAError as e:
+            assert e.code == pa.PA_ERR_INVALID_ARG
+        else:
+            raise AssertionError("accepted n=%d v=%d" % (n, v))
+
+
+def test_error_strings(pa_lib):
+    assert pa.error_string(pa.PA_OK) == "ok"
+    assert "seed" in pa.error_string(pa.PA_ERR_NO_SEED)
