@@ -288,10 +288,15 @@ static int check_n(pa_engine* e, uint32_t n, uint32_t v, uint32_t flags, BlockGe
     return PA_OK;
 }
 
+// Seed sizes: any block size the engine accepts (the output length is only known per key block).
+static int check_seed_n(pa_engine* e, uint32_t n) {
+    BlockGeom g;
+    return check_n(e, n, 32u, PA_FLAG_COMPRESS, &g);
+}
+
 int pa_set_seed(pa_engine* e, const uint32_t* seed_words, uint32_t n, int32_t reuse_seed_amount) {
     if (!e || !seed_words) return PA_ERR_INVALID_ARG;
-    BlockGeom g;
-    int rc = check_n(e, n, n / 2u, PA_FLAG_COMPRESS, &g);
+    int rc = check_seed_n(e, n);
     if (rc) return rc;
     PA_CUDA(e, cudaSetDevice(e->device));
     PA_CUDA(e, cudaMemcpyAsync(e->d_seed, seed_words, (size_t)(n / 32u) * 4u, cudaMemcpyHostToDevice, e->stream));
@@ -304,8 +309,7 @@ int pa_set_seed(pa_engine* e, const uint32_t* seed_words, uint32_t n, int32_t re
 int pa_set_seed_device(pa_engine* e, const uint32_t* d_seed_words, uint32_t n, int32_t reuse_seed_amount,
                        void* stream) {
     if (!e || !d_seed_words) return PA_ERR_INVALID_ARG;
-    BlockGeom g;
-    int rc = check_n(e, n, n / 2u, PA_FLAG_COMPRESS, &g);
+    int rc = check_seed_n(e, n);
     if (rc) return rc;
     cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
     PA_CUDA(e, cudaSetDevice(e->device));

@@ -125,10 +125,19 @@ def test_rejects_bad_sizes(gpu_engine):
     seed, recv = O.random_block(4096, 1536, 1)
     gpu_engine.set_seed(seed, 4096, -1)
     ks, kr = O.key_split(recv, 4096, 1536)
-    for n, v in [(4096, 0), (4096, 4096), (4096, 100), (4000, 1536), (512, 256)]:
+    # buffers large enough for any (n, v) below, so that the C ABI's own checks decide
+    ks_big = np.concatenate([ks, np.zeros(8, np.uint32)])
+    kr_big = np.concatenate([kr, np.zeros(4096 // 32, np.uint32)])
+    for n, v in [(4096, 0), (4096, 4096), (4096, 100), (4000, 1536), (512, 256), (4096, 4064 + 64)]:
         with pytest.raises(pa.PAError) as ei:
-            gpu_engine.process(ks, kr, n, v)
-        assert ei.value.code in (pa.PA_ERR_INVALID_ARG, pa.PA_ERR_NO_SEED)
+            gpu_engine.process(ks_big, kr_big, n, v)
+        assert ei.value.code == pa.PA_ERR_INVALID_ARG, (n, v)
+    with pytest.raises(pa.PAError) as ei:
+        gpu_engine.set_seed(np.zeros((1 << 28) // 32, np.uint32), 1 << 28, -1)
+    assert ei.value.code in (pa.PA_ERR_TOO_LARGE, pa.PA_ERR_INVALID_ARG)
+    # the engine still works after rejected calls
+    gpu_engine.set_seed(seed, 4096, -1)
+    assert np.array_equal(gpu_engine.process(ks, kr, 4096, 1536), O.direct(seed, ks, kr, 4096, 1536))
 
 
 def test_popcounts_reported(gpu_engine):
