@@ -34,9 +34,6 @@ struct pa_engine {
     uint32_t* d_planes = nullptr;
     unsigned long long* d_cnt = nullptr;  // [0] key popcount, [1] seed popcount
     unsigned int* d_resid = nullptr;
-    float2* d_glo = nullptr;
-    float2* d_ghi = nullptr;
-    int tw_log_n = -1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // seed state
     bool seed_valid = false;
@@ -94,7 +91,7 @@ int make_geom(uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
     if (g->log_n <= 14) {
         g->log_n1 = g->log_n2 = 0;
     } else {
-        g->log_n2 = std::min(14, g->log_n - 6);
+        g->log_n2 = std::min(14, g->log_n - 5);  // rows 2^10..2^14, columns 2^5..2^12
         g->log_n1 = g->log_n - g->log_n2;
     }
     if (g->log_n1 > 12) return PA_ERR_TOO_LARGE;
@@ -107,18 +104,8 @@ bool same_seed_geom(const BlockGeom& a, const BlockGeom& b) {
     return a.seed_direct == b.seed_direct && a.h == b.h;
 }
 
-int ensure_twiddles(pa_engine* e, const BlockGeom& g, cudaStream_t s) {
-    if (g.log_n1 == 0 || e->tw_log_n == g.log_n) return PA_OK;
-    int rc = pa::launch_twiddle_tables(g, e->d_glo, e->d_ghi, s);
-    if (rc) return cuda_fail(e, (cudaError_t)rc);
-    e->tw_log_n = g.log_n;
-    return PA_OK;
-}
-
 int build_spectrum(pa_engine* e, const BlockGeom& g, cudaStream_t s) {
-    int rc = ensure_twiddles(e, g, s);
-    if (rc) return rc;
-    rc = pa::launch_seed_spectrum(g, e->d_seed, e->d_spec, e->d_work, e->d_cnt + 1, {e->d_glo, e->d_ghi}, s);
+    int rc = pa::launch_seed_spectrum(g, e->d_seed, e->d_spec, e->d_work, e->d_planes, e->d_cnt + 1, e->num_sms, s);
     if (rc) return cuda_fail(e, (cudaError_t)rc);
     e->spec_geom = g;
     e->spec_valid = true;
@@ -147,19 +134,17 @@ int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const
         int rc = build_spectrum(e, g, s);
         if (rc) return rc;
     }
-    int rc = ensure_twiddles(e, g, s);
-    if (rc) return rc;
     PA_CUDA(e, cudaEventRecord(e->ev0, s));
     cudaEvent_t* sev = nullptr;
     if (e->timing && !e->tev.empty()) {
         size_t slot = e->tev_next;
         sev = e->tev[slot].data();
-        e->tev_stages[slot] = pa::kernel_count_key_block(g);
+        e->tev_stages[slot] = pa::stage_count_key_block(g);
         e->tev_next = (slot + 1) % e->tev.size();
         e->tev_count = std::min(e->tev_count + 1, e->tev.size());
     }
-    rc = pa::launch_key_block(g, d_ks, d_kr, flags, e->d_spec, e->d_work, e->d_planes, e->d_cnt, e->d_resid, d_out,
-                              {e->d_glo, e->d_ghi}, e->num_sms, s, sev);
+    int rc = pa::launch_key_block(g, d_ks, d_kr, flags, e->d_spec, e->d_work, e->d_planes, e->d_cnt, e->d_resid,
+                                  d_out, e->num_sms, s, sev);
     if (rc) return cuda_fail(e, (cudaError_t)rc);
     PA_CUDA(e, cudaEventRecord(e->ev1, s));
     if (e->seed_left > 0) --e->seed_left;
@@ -250,8 +235,6 @@ int pa_create(const pa_config* cfg, pa_engine** out) {
     if ((err = cudaMalloc(&e->d_planes, np / 8 + 256)) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_cnt, 2 * sizeof(unsigned long long))) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_resid, sizeof(unsigned int))) != cudaSuccess) return fail(err);
-    if ((err = cudaMalloc(&e->d_glo, 8192 * sizeof(float2))) != cudaSuccess) return fail(err);
-    if ((err = cudaMalloc(&e->d_ghi, 16384 * sizeof(float2))) != cudaSuccess) return fail(err);
     cudaMemset(e->d_cnt, 0, 2 * sizeof(unsigned long long));
     cudaMemset(e->d_resid, 0, sizeof(unsigned int));
     *out = e;
@@ -271,8 +254,6 @@ void pa_destroy(pa_engine* e) {
     cudaFree(e->d_planes);
     cudaFree(e->d_cnt);
     cudaFree(e->d_resid);
-    cudaFree(e->d_glo);
-    cudaFree(e->d_ghi);
     for (auto& a : e->tev)
         for (auto ev : a) cudaEventDestroy(ev);
     if (e->ev0) cudaEventDestroy(e->ev0);

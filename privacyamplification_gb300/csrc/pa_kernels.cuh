@@ -32,21 +32,28 @@ __host__ __device__ inline int seed_source(const BlockGeom& g, uint64_t x, uint6
 
 // Host launch API (pa_kernels.cu).  All launches are asynchronous on `stream`.
 namespace pa {
-struct DeviceTables {
-    const float2* glo;  // W_N^a, a < 8192
-    const float2* ghi;  // W_N^(8192 b), b < max(1, N/8192)
-};
-int launch_twiddle_tables(const BlockGeom& g, float2* glo, float2* ghi, cudaStream_t s);
-// Seed spectrum (FP32, scaled by 1/(2Np)) in the layout the key path consumes; work is scratch of
-// N complex (three-pass path only).  cnt_seed receives the popcount of the placed seed.
-int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec, float2* work,
-                         unsigned long long* cnt_seed, DeviceTables tw, cudaStream_t s);
+// Seed spectrum (FP32, scaled by 1/(2Np)) in the layout the key path consumes.  work (N complex) and
+// rows (Np/8 bytes) are scratch of the three-pass path.  cnt_seed receives the popcount of the
+// placed seed.
+int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec, float2* work, uint32_t* rows,
+                         unsigned long long* cnt_seed, int num_sms, cudaStream_t s);
 // Key block: out_words receives ceil(out_bits/32) little-endian words of the reference byte stream.
 // stage_ev (optional, kernel_count_key_block()+1 events) is recorded before the first kernel and
-// after each kernel.
+// after each stage.
 int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32_t* key_rest, uint32_t flags,
                      const float2* spec, float2* work, uint32_t* planes, unsigned long long* cnt,
-                     unsigned int* resid_bits, uint32_t* out_words, DeviceTables tw, int num_sms,
-                     cudaStream_t s, cudaEvent_t* stage_ev);
-int kernel_count_key_block(const BlockGeom& g);
+                     unsigned int* resid_bits, uint32_t* out_words, int num_sms, cudaStream_t s,
+                     cudaEvent_t* stage_ev);
+int kernel_count_key_block(const BlockGeom& g);   // kernels one key block launches
+int stage_count_key_block(const BlockGeom& g);    // timed stages (events - 1) of a key block
+
+// Three-pass kernels (pa_passes.cu).  `rows` and the parity planes share one buffer of Np/8 bytes.
+int launch_bit_rows(const BlockGeom& g, const uint32_t* bits, bool seed, uint32_t* rows, cudaStream_t s);
+int launch_pass_a(const BlockGeom& g, const uint32_t* rows, bool seed, float2* Y, unsigned long long* cnt,
+                  int num_sms, cudaStream_t s);
+int launch_pass_b(const BlockGeom& g, bool seed, float2* Y, float2* spec, int num_sms, cudaStream_t s);
+int launch_pass_c(const BlockGeom& g, const float2* Y, const unsigned long long* cnt, uint32_t* planes,
+                  unsigned int* resid, int num_sms, cudaStream_t s);
+int launch_finish(const BlockGeom& g, const uint32_t* planes, const uint32_t* key_rest, uint32_t flags,
+                  uint32_t* out, cudaStream_t s);
 }  // namespace pa
