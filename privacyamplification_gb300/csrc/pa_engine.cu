@@ -29,8 +29,12 @@ struct pa_engine {
     uint32_t* d_key_rest = nullptr;
     uint32_t* d_seed = nullptr;
     uint32_t* d_out = nullptr;
-    float2* d_work = nullptr;
+    float2* d_work = nullptr;   // pass A output (row-major)
+    float2* d_work2 = nullptr;  // pass B output (tile-major)
     float2* d_spec = nullptr;
+    int* d_err = nullptr;       // device error word of the bounded TMA waits
+    pa::PassMaps maps{};        // tensor maps for the geometry maps_log_n
+    int maps_log_n = -1;
     uint32_t* d_planes = nullptr;
     unsigned long long* d_cnt = nullptr;  // [0] key popcount, [1] seed popcount
     unsigned int* d_resid = nullptr;
@@ -104,8 +108,20 @@ bool same_seed_geom(const BlockGeom& a, const BlockGeom& b) {
     return a.seed_direct == b.seed_direct && a.h == b.h;
 }
 
+int ensure_maps(pa_engine* e, const BlockGeom& g) {
+    if (g.log_n1 == 0 || e->maps_log_n == g.log_n) return PA_OK;
+    int rc = pa::make_pass_maps(g, e->d_work, e->d_work2, &e->maps);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    e->maps_log_n = g.log_n;
+    return PA_OK;
+}
+
+pa::Scratch scratch(pa_engine* e) { return {e->d_work, e->d_work2, e->d_planes, e->d_err, &e->maps}; }
+
 int build_spectrum(pa_engine* e, const BlockGeom& g, cudaStream_t s) {
-    int rc = pa::launch_seed_spectrum(g, e->d_seed, e->d_spec, e->d_work, e->d_planes, e->d_cnt + 1, e->num_sms, s);
+    int rc = ensure_maps(e, g);
+    if (rc) return rc;
+    rc = pa::launch_seed_spectrum(g, e->d_seed, e->d_spec, scratch(e), e->d_cnt + 1, e->num_sms, s);
     if (rc) return cuda_fail(e, (cudaError_t)rc);
     e->spec_geom = g;
     e->spec_valid = true;
@@ -134,6 +150,8 @@ int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const
         int rc = build_spectrum(e, g, s);
         if (rc) return rc;
     }
+    int mrc = ensure_maps(e, g);
+    if (mrc) return mrc;
     PA_CUDA(e, cudaEventRecord(e->ev0, s));
     cudaEvent_t* sev = nullptr;
     if (e->timing && !e->tev.empty()) {
@@ -143,8 +161,8 @@ int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const
         e->tev_next = (slot + 1) % e->tev.size();
         e->tev_count = std::min(e->tev_count + 1, e->tev.size());
     }
-    int rc = pa::launch_key_block(g, d_ks, d_kr, flags, e->d_spec, e->d_work, e->d_planes, e->d_cnt, e->d_resid,
-                                  d_out, e->num_sms, s, sev);
+    int rc = pa::launch_key_block(g, d_ks, d_kr, flags, e->d_spec, scratch(e), e->d_cnt, e->d_resid, d_out,
+                                  e->num_sms, s, sev);
     if (rc) return cuda_fail(e, (cudaError_t)rc);
     PA_CUDA(e, cudaEventRecord(e->ev1, s));
     if (e->seed_left > 0) --e->seed_left;
@@ -156,6 +174,13 @@ int read_stats(pa_engine* e, pa_stats* st, float* resid_out) {
     unsigned int rb = 0;
     PA_CUDA(e, cudaMemcpy(cnt, e->d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost));
     PA_CUDA(e, cudaMemcpy(&rb, e->d_resid, sizeof(rb), cudaMemcpyDeviceToHost));
+    int derr = 0;
+    PA_CUDA(e, cudaMemcpy(&derr, e->d_err, sizeof(derr), cudaMemcpyDeviceToHost));
+    if (derr) {  // a bounded device wait expired: the block's result is not valid
+        cudaMemset(e->d_err, 0, sizeof(int));
+        e->last_cuda = (int)cudaErrorLaunchTimeout;
+        return PA_ERR_CUDA;
+    }
     float resid;
     std::memcpy(&resid, &rb, sizeof(resid));
     *resid_out = resid;
@@ -232,6 +257,9 @@ int pa_create(const pa_config* cfg, pa_engine** out) {
     if ((err = cudaMalloc(&e->d_out, words * 4)) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_work, (np / 2) * sizeof(float2))) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_spec, (np / 2) * sizeof(float2))) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_work2, (np / 2) * sizeof(float2))) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_err, sizeof(int))) != cudaSuccess) return fail(err);
+    cudaMemset(e->d_err, 0, sizeof(int));
     if ((err = cudaMalloc(&e->d_planes, np / 8 + 256)) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_cnt, 2 * sizeof(unsigned long long))) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_resid, sizeof(unsigned int))) != cudaSuccess) return fail(err);
@@ -251,6 +279,8 @@ void pa_destroy(pa_engine* e) {
     cudaFree(e->d_out);
     cudaFree(e->d_work);
     cudaFree(e->d_spec);
+    cudaFree(e->d_work2);
+    cudaFree(e->d_err);
     cudaFree(e->d_planes);
     cudaFree(e->d_cnt);
     cudaFree(e->d_resid);

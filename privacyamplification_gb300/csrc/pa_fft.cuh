@@ -9,11 +9,28 @@
 //   MapMirrorRow   NSEQ == 1, R == 16: q = 0 -> j = tid, q = 1 -> j = L/16 - tid (tid 0: L/32)
 //   MapMirrorPair  NSEQ even, R == 16: tid -> pair pp = tid / (L/16), jj = tid % (L/16);
 //                  q = 0 -> (2pp, jj), q = 1 -> (2pp+1, L/16-1-jj)
-// The mirror maps put bin k and its real-FFT partner in the same thread (see pa_kernels.cu).
+// The mirror maps put bin k and its real-FFT partner in the same thread (see pa_passes.cu).
+//
+// Shared-memory positions are padded, k -> k + (k >> S) with S = 4 or 5 per exchange: S = 5 for the
+// exchange after a radix-32 stage with NS = 1 (stride-32 writes), S = 4 otherwise.  For every
+// stage shape used here pad(o + r*D) = pad(o) + r*D + (r*D >> S), so each thread computes one base
+// address per butterfly and all R accesses use constant offsets.
 #pragma once
 #include "pa_device.cuh"
 
 namespace pa {
+
+template <int S>
+__device__ __forceinline__ constexpr int padk(int k) { return k + (k >> S); }
+template <int S>
+__device__ __forceinline__ constexpr int padoff(int d) { return d + (d >> S); }
+
+// Sequence stride of a tile in shared memory (elements): room for pad16, rounded to 4 mod 16 so that
+// neighbouring columns written by one half-warp fall on different banks.
+template <int L>
+struct TileStride {
+    static constexpr int value = (L + L / 16 + 11) / 16 * 16 + 4;  // smallest s >= L + L/16, s = 4 mod 16
+};
 
 template <int NT>
 struct MapLinear {
@@ -79,71 +96,77 @@ __device__ __forceinline__ float2 unit_root(int t, int M) {
     return make_float2(c, s);
 }
 
-// Stage compute: twiddles (NS > 1) then radix-R DFTs of the thread's Q = E/R butterflies.
-template <int L, int R, int NS, int DIR, int E, class Map>
-__device__ __forceinline__ void stage(float2 (&x)[E]) {
+// Stage compute: twiddles (NS > 1, bases w[q] = W_{NS R}^{DIR (j mod NS)} precomputed by the caller)
+// then radix-R DFTs of the thread's Q = E/R butterflies.
+template <int R, int NS, int DIR, int E>
+__device__ __forceinline__ void stage(float2 (&x)[E], const float2* w) {
     constexpr int Q = E / R;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        if (NS > 1) {
-            int seq, j;
-            Map::template at<L, R>(q, seq, j);
-            twiddle_powers<R, false>(&x[q * R], unit_root<DIR>(j % NS, NS * R), make_float2(1.f, 0.f));
-        }
+        if (NS > 1) twiddle_powers<R, false>(&x[q * R], w[q], make_float2(1.f, 0.f));
         dft<R, DIR>(reinterpret_cast<float2(&)[R]>(x[q * R]));
     }
 }
 
+// Twiddle bases of a stage for the thread's butterflies: w[q] = W_{NS R}^{DIR (j_q mod NS)}.
+template <int L, int R, int NS, int DIR, int E, class Map>
+__device__ __forceinline__ void stage_bases(float2* w) {
+#pragma unroll
+    for (int q = 0; q < E / R; ++q) {
+        int seq, j;
+        Map::template at<L, R>(q, seq, j);
+        w[q] = unit_root<DIR>(j % NS, NS * R);
+    }
+}
+
 // Exchange between stage A (radix RA, NSA, map MA: its outputs) and stage B (radix RB, map MB: its
-// inputs) through the shared tile sm (sequence stride Padded<L>).  Starts with a barrier so that
-// earlier reads of sm are complete.
-template <int L, int E, int RA, int NSA, class MA, int RB, class MB>
+// inputs) through the shared tile sm (sequence stride SP, padding shift S).  Starts with a barrier
+// so that earlier reads of sm are complete.
+template <int L, int SP, int S, int E, int RA, int NSA, class MA, int RB, class MB>
 __device__ __forceinline__ void exchange(float2 (&x)[E], float2* sm) {
-    constexpr int SP = Padded<L>::value;
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < E / RA; ++q) {
         int seq, j;
         MA::template at<L, RA>(q, seq, j);
-        const int base = seq * SP + 0;
-        const int o = (j / NSA) * NSA * RA + (j % NSA);
+        float2* b = sm + seq * SP + padk<S>((j / NSA) * NSA * RA + (j % NSA));
 #pragma unroll
-        for (int r = 0; r < RA; ++r) sm[base + pad16(o + r * NSA)] = x[q * RA + r];
+        for (int r = 0; r < RA; ++r) b[padoff<S>(r * NSA)] = x[q * RA + r];
     }
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < E / RB; ++q) {
         int seq, j;
         MB::template at<L, RB>(q, seq, j);
-        const int base = seq * SP;
+        const float2* b = sm + seq * SP + padk<S>(j);
 #pragma unroll
-        for (int r = 0; r < RB; ++r) x[q * RB + r] = sm[base + pad16(j + r * (L / RB))];
+        for (int r = 0; r < RB; ++r) x[q * RB + r] = b[padoff<S>(r * (L / RB))];
     }
 }
 
-// Reads the inputs of a first stage (radix R, map M) from the tile.
-template <int L, int E, int R, class M>
+// Reads the inputs of a first stage (radix R, map M) from a tile stored with pad16.
+template <int L, int SP, int E, int R, class M>
 __device__ __forceinline__ void gather_inputs(float2 (&x)[E], const float2* sm) {
-    constexpr int SP = Padded<L>::value;
 #pragma unroll
     for (int q = 0; q < E / R; ++q) {
         int seq, j;
         M::template at<L, R>(q, seq, j);
+        const float2* b = sm + seq * SP + padk<4>(j);
 #pragma unroll
-        for (int r = 0; r < R; ++r) x[q * R + r] = sm[seq * SP + pad16(j + r * (L / R))];
+        for (int r = 0; r < R; ++r) x[q * R + r] = b[padoff<4>(r * (L / R))];
     }
 }
 
-// Writes the outputs of a last stage (radix R, NS = L/R, map M) to the tile in natural order.
-template <int L, int E, int R, class M>
+// Writes the outputs of a last stage (radix R, NS = L/R, map M) to the tile in natural order, pad16.
+template <int L, int SP, int E, int R, class M>
 __device__ __forceinline__ void scatter_outputs(const float2 (&x)[E], float2* sm) {
-    constexpr int SP = Padded<L>::value;
 #pragma unroll
     for (int q = 0; q < E / R; ++q) {
         int seq, j;
         M::template at<L, R>(q, seq, j);
+        float2* b = sm + seq * SP + padk<4>(j);
 #pragma unroll
-        for (int r = 0; r < R; ++r) sm[seq * SP + pad16(j + r * (L / R))] = x[q * R + r];
+        for (int r = 0; r < R; ++r) b[padoff<4>(r * (L / R))] = x[q * R + r];
     }
 }
 
@@ -156,6 +179,12 @@ struct Plan {
     static constexpr int RA = 1 << (NSTAGE == 1 ? REST : (REST + 1) / 2);
     static constexpr int RB = NSTAGE == 1 ? 1 : 1 << (REST / 2);
     static_assert(REST >= 1 && REST <= 10, "transform length out of range");
+};
+
+// Padding shift of an exchange that follows a stage of radix R with NS = 1.
+template <int R>
+struct PadAfterFirst {
+    static constexpr int value = R == 32 ? 5 : 4;
 };
 
 }  // namespace pa

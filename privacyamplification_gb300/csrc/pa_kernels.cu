@@ -251,7 +251,7 @@ static int mono_key(const BlockGeom& g, const uint32_t* ks, const uint32_t* kr, 
         default: return (int)cudaErrorInvalidValue; \
     }
 
-int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec, float2* work, uint32_t* rows,
+int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec, const Scratch& sc,
                          unsigned long long* cnt_seed, int num_sms, cudaStream_t s) {
     if (g.log_n1 == 0) {
 #define C(NN) mono_seed<NN>(g, seed, spec, cnt_seed, s)
@@ -259,16 +259,15 @@ int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec,
 #undef C
     }
     cudaMemsetAsync(cnt_seed, 0, sizeof(unsigned long long), s);
-    int rc = launch_bit_rows(g, seed, true, rows, s);
-    if (!rc) rc = launch_pass_a(g, rows, true, work, cnt_seed, num_sms, s);
-    if (!rc) rc = launch_pass_b(g, true, work, spec, num_sms, s);
+    int rc = launch_bit_rows(g, seed, true, sc.planes, s);
+    if (!rc) rc = launch_pass_a(g, sc.planes, true, sc.work, cnt_seed, num_sms, s);
+    if (!rc) rc = launch_pass_b(g, true, *sc.maps, sc.work, sc.work2, spec, sc.err, num_sms, s);
     return rc;
 }
 
 int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32_t* key_rest, uint32_t flags,
-                     const float2* spec, float2* work, uint32_t* planes, unsigned long long* cnt,
-                     unsigned int* resid_bits, uint32_t* out_words, int num_sms, cudaStream_t s,
-                     cudaEvent_t* ev) {
+                     const float2* spec, const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits,
+                     uint32_t* out_words, int num_sms, cudaStream_t s, cudaEvent_t* ev) {
     auto mark = [&](int i) {
         if (ev) cudaEventRecord(ev[i], s);
     };
@@ -284,14 +283,14 @@ int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32
     }
     cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s);  // key popcount; cnt[1] is the seed's
     mark(0);
-    int rc = launch_bit_rows(g, key_start, false, planes, s);
-    if (!rc) rc = launch_pass_a(g, planes, false, work, cnt, num_sms, s);
+    int rc = launch_bit_rows(g, key_start, false, sc.planes, s);
+    if (!rc) rc = launch_pass_a(g, sc.planes, false, sc.work, cnt, num_sms, s);
     mark(1);
-    if (!rc) rc = launch_pass_b(g, false, work, const_cast<float2*>(spec), num_sms, s);
+    if (!rc) rc = launch_pass_b(g, false, *sc.maps, sc.work, sc.work2, const_cast<float2*>(spec), sc.err, num_sms, s);
     mark(2);
-    if (!rc) rc = launch_pass_c(g, work, cnt, planes, resid_bits, num_sms, s);
+    if (!rc) rc = launch_pass_c(g, *sc.maps, sc.work2, cnt, sc.planes, resid_bits, sc.err, num_sms, s);
     mark(3);
-    if (!rc) rc = launch_finish(g, planes, key_rest, flags, out_words, s);
+    if (!rc) rc = launch_finish(g, sc.planes, key_rest, flags, out_words, s);
     mark(4);
     return rc;
 }

@@ -1,5 +1,6 @@
 // pa_kernels.cuh -- block geometry shared by the host engine and the kernels.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -35,15 +36,22 @@ namespace pa {
 // Seed spectrum (FP32, scaled by 1/(2Np)) in the layout the key path consumes.  work (N complex) and
 // rows (Np/8 bytes) are scratch of the three-pass path.  cnt_seed receives the popcount of the
 // placed seed.
-int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec, float2* work, uint32_t* rows,
+struct PassMaps;
+struct Scratch {
+    float2* work;       // N complex: pass A output (row-major)
+    float2* work2;      // N complex: pass B output (tile-major)
+    uint32_t* planes;   // Np/8 bytes: input bit rows, then parity planes
+    int* err;           // device error word (bounded waits)
+    const PassMaps* maps;
+};
+int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec, const Scratch& sc,
                          unsigned long long* cnt_seed, int num_sms, cudaStream_t s);
 // Key block: out_words receives ceil(out_bits/32) little-endian words of the reference byte stream.
 // stage_ev (optional, kernel_count_key_block()+1 events) is recorded before the first kernel and
 // after each stage.
 int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32_t* key_rest, uint32_t flags,
-                     const float2* spec, float2* work, uint32_t* planes, unsigned long long* cnt,
-                     unsigned int* resid_bits, uint32_t* out_words, int num_sms, cudaStream_t s,
-                     cudaEvent_t* stage_ev);
+                     const float2* spec, const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits,
+                     uint32_t* out_words, int num_sms, cudaStream_t s, cudaEvent_t* stage_ev);
 int kernel_count_key_block(const BlockGeom& g);   // kernels one key block launches
 int stage_count_key_block(const BlockGeom& g);    // timed stages (events - 1) of a key block
 
@@ -51,9 +59,15 @@ int stage_count_key_block(const BlockGeom& g);    // timed stages (events - 1) o
 int launch_bit_rows(const BlockGeom& g, const uint32_t* bits, bool seed, uint32_t* rows, cudaStream_t s);
 int launch_pass_a(const BlockGeom& g, const uint32_t* rows, bool seed, float2* Y, unsigned long long* cnt,
                   int num_sms, cudaStream_t s);
-int launch_pass_b(const BlockGeom& g, bool seed, float2* Y, float2* spec, int num_sms, cudaStream_t s);
-int launch_pass_c(const BlockGeom& g, const float2* Y, const unsigned long long* cnt, uint32_t* planes,
-                  unsigned int* resid, int num_sms, cudaStream_t s);
+struct PassMaps {
+    CUtensorMap y;  // Y (pass A output, row-major) as read by pass B
+    CUtensorMap z;  // Z (pass B output, tile-major) as read by pass C
+};
+int make_pass_maps(const BlockGeom& g, const float2* Y, const float2* Z, PassMaps* out);
+int launch_pass_b(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y, float2* Z, float2* spec, int* err,
+                  int num_sms, cudaStream_t s);
+int launch_pass_c(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
+                  uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s);
 int launch_finish(const BlockGeom& g, const uint32_t* planes, const uint32_t* key_rest, uint32_t flags,
                   uint32_t* out, cudaStream_t s);
 }  // namespace pa

@@ -13,8 +13,12 @@
 #include "pa_device.cuh"
 #include "pa_fft.cuh"
 #include "pa_kernels.cuh"
+#include "pa_tma.cuh"
+
+#include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstring>
 
 namespace pa {
 
@@ -60,15 +64,43 @@ __device__ __forceinline__ float block_max_f(float v, float* red) {
     return t;
 }
 
+// Asynchronous prefetch of [p, p + bytes) into L2 (bytes a multiple of 16, p 16-byte aligned).
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// 8-byte asynchronous global -> shared copy (L2 only), and the wait for all of a thread's copies.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t load_bit(const uint32_t* __restrict__ w, uint64_t x) {
     return (__ldg(w + (x >> 5)) >> (31u - (uint32_t)(x & 31u))) & 1u;
 }
 
 }  // namespace
 
-// ============================================================================ input bit planes
-// Warp (a, c): rows m1 = 16a .. 16a+15, columns m2 = 32c .. 32c+31 (lane = m2 - 32c).  The lane's
-// input word holds the 32 bits x = 2 N1 m2 + 32a + [0, 32) = bit pairs of rows 16a..16a+15.
+// ============================================================================ bit-plane transposes
+// 16 x 16 transpose of 2-bit elements inside each half-warp (Eklundh's recursive block swap):
+// element e of lane L (bits 31-2e and 30-2e) becomes element L of lane e.
+__device__ __forceinline__ uint32_t transpose16x2(uint32_t w, int lane) {
+    const uint32_t masks[4] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u};  // elements with e & s
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int s = 8 >> i;
+        const uint32_t m = masks[i];
+        const uint32_t p = __shfl_xor_sync(0xffffffffu, w, s);
+        w = (lane & s) ? ((w & m) | ((p & m) << (2 * s))) : ((w & ~m) | ((p & ~m) >> (2 * s)));
+    }
+    return w;
+}
+
+// Input bit planes.  Warp (a, c): rows m1 = 16a .. 16a+15, columns m2 = 32c .. 32c+31 (lane = m2 - 32c).
+// The lane's input word holds x = 2 N1 m2 + 32a + [0, 32), i.e. 16 (even, odd) pairs of rows
+// 16a..16a+15; after the half-warp transpose, lane L of half h holds row 16a + L, columns
+// 32c + 16h .. 32c + 16h + 15 -- one word of the row plane.
 template <bool SEED>
 __global__ void __launch_bounds__(256) k_bit_rows(const uint32_t* __restrict__ src, BlockGeom g,
                                                   uint32_t* __restrict__ rows) {
@@ -93,44 +125,61 @@ __global__ void __launch_bounds__(256) k_bit_rows(const uint32_t* __restrict__ s
             if (seed_source(g, x0 + b, &s)) v |= load_bit(src, s) << (31 - b);
         }
     }
-    uint32_t mine = 0;
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-        uint32_t e = __ballot_sync(0xffffffffu, (v >> (31 - 2 * u)) & 1u);
-        uint32_t o = __ballot_sync(0xffffffffu, (v >> (30 - 2 * u)) & 1u);
-        if ((lane >> 1) == u) mine = (lane & 1) ? msb_pairs(e >> 16, o >> 16) : msb_pairs(e, o);
-    }
-    const uint32_t row = 16u * a + (uint32_t)(lane >> 1);
-    rows[(size_t)row * (n2 / 16u) + 2u * c + (uint32_t)(lane & 1)] = mine;
+    const uint32_t w = transpose16x2(v, lane);
+    rows[(size_t)(16u * a + (uint32_t)(lane & 15)) * (n2 / 16u) + 2u * c + (uint32_t)(lane >> 4)] = w;
 }
 
 // ============================================================================ pass A
 // Row m1: FFT over m2 of the 2N2 bits of the row, 4-step twiddle W_N^{m1 k2}, pair-order store.
+// Radices RA, RB (linear) then 16 (mirror, NS = L/16).
 template <int LOGL, bool SEED>
 __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     k_pass_a(const uint32_t* __restrict__ rows, BlockGeom g, float2* __restrict__ Y, unsigned long long* cnt) {
-    constexpr int L = 1 << LOGL, NT = L / 32, E = 32, LR = L / 16;
+    constexpr int L = 1 << LOGL, NT = L / 32, E = 32, LR = L / 16, SP = TileStride<L>::value;
     using P = Plan<LOGL>;
     using Lin = MapLinear<NT>;
+    constexpr int QB = P::NSTAGE == 2 ? E / P::RB : 0;   // butterflies per thread in stage B
+    constexpr int T1N = LR < 32 ? LR : 32, T2N = LR / T1N;  // W_N^{m1 j} = T1[j % 32] T2[j / 32]
     extern __shared__ float2 sm[];
-    __shared__ float2 rho[16];
+    __shared__ float2 rho[16], t1[T1N], t2[T2N];
+    __shared__ float2 tws[(QB > 0 ? QB : 1) + 2][NT];
     __shared__ uint32_t bits[L / 16];
     __shared__ unsigned long long red[32];
     const uint32_t n1 = 1u << g.log_n1;
     const int t = threadIdx.x;
+    // per-thread stage twiddle bases (the same for every row)
+    float2 wb[QB > 0 ? QB : 1], wm[2];
+    if (P::NSTAGE == 2) stage_bases<L, P::RB, P::RA, -1, E, Lin>(wb);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        int seq, j;
+        MapMirrorRow::at<L, 16>(q, seq, j);
+        wm[q] = unit_root<-1>(j, L);
+    }
+#pragma unroll
+    for (int q = 0; q < QB; ++q) tws[q][t] = wb[q];
+    tws[QB][t] = wm[0];
+    tws[QB + 1][t] = wm[1];
     uint32_t ones = 0;
     for (uint32_t m1 = blockIdx.x; m1 < n1; m1 += gridDim.x) {
-        __syncthreads();  // previous row done with bits / rho / sm
+        __syncthreads();  // previous row done with bits / tables / sm
         const uint32_t* rw = rows + (size_t)m1 * (L / 16);
-        for (int i = t; i < L / 16; i += NT) {
-            uint32_t w = __ldg(rw + i);
-            bits[i] = w;
+#pragma unroll
+        for (int i = 0; i < L / 16 / NT; ++i) {
+            uint32_t w = __ldg(rw + t + i * NT);
+            bits[t + i * NT] = w;
             ones += __popc(w);
         }
-        if (t < 16) rho[t] = expmi_pi((uint32_t)((2ull * m1 * LR * (uint64_t)t) & ((2ull << g.log_n) - 1)), g.log_n);
+        for (int i = t; i < 16 + T1N + T2N; i += NT) {  // W_N^{m1 LR r}, W_N^{m1 i}, W_N^{m1 T1N i}
+            uint64_t e = i < 16 ? (uint64_t)LR * (uint64_t)i : (i < 16 + T1N ? (uint64_t)(i - 16)
+                                                                                : (uint64_t)T1N * (uint64_t)(i - 16 - T1N));
+            float2 w = expmi_pi((uint32_t)((2ull * m1 * e) & ((2ull << g.log_n) - 1)), g.log_n);
+            if (i < 16) rho[i] = w;
+            else if (i < 16 + T1N) t1[i - 16] = w;
+            else t2[i - 16 - T1N] = w;
+        }
         __syncthreads();
         float2 x[E];
-        // first stage inputs: butterfly u = t + q*NT, element m2 = u + r*(L/RA)
 #pragma unroll
         for (int q = 0; q < E / P::RA; ++q) {
             const int j = t + q * NT;
@@ -142,13 +191,16 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
                 x[q * P::RA + r] = make_float2((float)((w >> (sh + 1)) & 1u), (float)((w >> sh) & 1u));
             }
         }
-        stage<L, P::RA, 1, -1, E, Lin>(x);
+        stage<P::RA, 1, -1, E>(x, nullptr);
         if (P::NSTAGE == 2) {
-            exchange<L, E, P::RA, 1, Lin, P::RB, Lin>(x, sm);
-            stage<L, P::RB, P::RA, -1, E, Lin>(x);
-            exchange<L, E, P::RB, P::RA, Lin, 16, MapMirrorRow>(x, sm);
+            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm);
+            float2 w[QB > 0 ? QB : 1];
+#pragma unroll
+            for (int q = 0; q < QB; ++q) w[q] = tws[q][t];
+            stage<P::RB, P::RA, -1, E>(x, w);
+            exchange<L, SP, 4, E, P::RB, P::RA, Lin, 16, MapMirrorRow>(x, sm);
         } else {
-            exchange<L, E, P::RA, 1, Lin, 16, MapMirrorRow>(x, sm);
+            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorRow>(x, sm);
         }
         // mirror stage (NS = L/16) with the 4-step twiddle W_N^{m1 (j + LR r)} folded in:
         // W_N^{m1 j} on the inputs, rho[r] = W_N^{m1 LR r} on the outputs.
@@ -156,8 +208,8 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
         for (int q = 0; q < 2; ++q) {
             int seq, j;
             MapMirrorRow::at<L, 16>(q, seq, j);
-            float2 c = expmi_pi(2u * m1 * (uint32_t)j, g.log_n);
-            twiddle_powers<16, true>(&x[16 * q], unit_root<-1>(j, L), c);
+            const float2 c = cmul(t1[j % T1N], t2[j / T1N]);
+            twiddle_powers<16, true>(&x[16 * q], tws[QB + q][t], c);
             dft<16, -1>(reinterpret_cast<float2(&)[16]>(x[16 * q]));
 #pragma unroll
             for (int r = 0; r < 16; ++r) x[16 * q + r] = cmul(x[16 * q + r], rho[r]);
@@ -201,51 +253,171 @@ __device__ __forceinline__ int spec_index(int c, int k1) {
     return (c * 16 + r) * LR + jj;
 }
 
+// 256 threads x 32 values: a tile is 8192 complex values (one mirror pair of 4096-point columns at
+// n = 2^27), so that two CTAs share an SM and hide each other's HBM latency.
+// Input: Y (row-major pairs, as pass A wrote it) through 2D TMA boxes of 256 rows x CPT columns, or
+// per-thread asynchronous copies when the tile is too wide for a box.  Output (key pass): Z, tile-major
+// (Z[tile][m1][CPT columns]), stored coalesced from registers; (seed pass): spec.
 template <int LOGL, bool SEED>
-__global__ void __launch_bounds__(512, 1)
-    k_pass_b(float2* __restrict__ Y, BlockGeom g, float2* __restrict__ spec) {
-    constexpr int L = 1 << LOGL, NT = 512, E = 32, CPT = 16384 / L, LR = L / 16, SP = Padded<L>::value;
-    constexpr int RL = Plan<LOGL>::RA;  // radix of the last inverse stage
+__global__ void __launch_bounds__(256, 2)
+    k_pass_b(const __grid_constant__ CUtensorMap mapY, const float2* __restrict__ Y, float2* __restrict__ Z,
+             BlockGeom g, float2* __restrict__ spec, int* err) {
+    constexpr int L = 1 << LOGL, NT = 256, E = 32, CPT = 8192 / L, LR = L / 16, SP = TileStride<L>::value;
+    constexpr bool TMA = CPT <= 128;              // box inner extent 2*CPT floats <= 256
+    constexpr int BOXR = L < 256 ? L : 256;       // rows per box
     using P = Plan<LOGL>;
     using Lin = MapLinear<NT>;
-    extern __shared__ float2 sm[];
-    float2* sigma = sm + CPT * SP;  // [CPT][RL] output twists of the last inverse stage
+    constexpr int RL = P::RA;                      // radix of the last inverse stage
+    constexpr int NSL = L / RL;                    // its NS
+    constexpr int QB = P::NSTAGE == 2 ? E / P::RB : 0;
+    constexpr int QL = E / RL;
+    // Short columns (many per tile): the last inverse stage computes its twiddles directly instead of
+    // keeping per-column tables, which would not fit in shared memory.
+    constexpr bool LEAN = LOGL <= 6;
+    constexpr int U1N = LEAN ? 0 : (NSL < 16 ? NSL : 16), U2N = LEAN ? 0 : NSL / U1N;  // W_N^{j k2}
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float2* sm = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    float2* sigma = sm + CPT * SP;       // [CPT][RL]   conj(W_N^{NSL r k2})
+    float2* u1 = sigma + CPT * RL;       // [CPT][U1N]  W_N^{k2 (j % 16)}
+    float2* u2 = u1 + CPT * U1N;         // [CPT][U2N]  W_N^{k2 16 (j / 16)}
+    float2* tws = u2 + CPT * U2N;        // [QB | 2 | QB | QL (unless LEAN)][NT] per-thread stage bases
+    constexpr int U1D = U1N > 0 ? U1N : 1, U2D = U2N > 0 ? U2N : 1;  // divisors (unused when LEAN)
+    __shared__ __align__(8) uint64_t bar;       // TMA completion of the current tile
+    __shared__ int s_fail;                      // a bounded wait expired: stop waiting
     const uint32_t n2 = 1u << g.log_n2;
     const int ntiles = (int)(n2 / CPT);
     const int t = threadIdx.x;
     const int pp = t / LR, jj = t % LR;
     const float sc = 1.0f / (float)(4ull << g.log_np);  // seed spectrum scale 2X/(4Np)
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        __syncthreads();  // previous tile done with sm
-        {   // coalesced load of the tile: row m1, pair cp -> columns 2cp, 2cp+1
-            const float4* Y4 = reinterpret_cast<const float4*>(Y);
-            for (int idx = t; idx < L * CPT / 2; idx += NT) {
-                int m1 = idx / (CPT / 2), cp = idx % (CPT / 2);
-                float4 v = __ldcs(Y4 + (((size_t)m1 * n2 + (size_t)tile * CPT) >> 1) + cp);
-                sm[(2 * cp) * SP + pad16(m1)] = make_float2(v.x, v.y);
-                sm[(2 * cp + 1) * SP + pad16(m1)] = make_float2(v.z, v.w);
+    {
+        float2 w[4];
+        if (P::NSTAGE == 2) {
+            stage_bases<L, P::RB, P::RA, -1, E, Lin>(w);
+#pragma unroll
+            for (int q = 0; q < QB; ++q) tws[q * NT + t] = w[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            int seq, j;
+            MapMirrorPair::at<L, 16>(q, seq, j);
+            tws[(QB + q) * NT + t] = unit_root<-1>(j, L);
+        }
+        if (P::NSTAGE == 2) {
+            stage_bases<L, P::RB, 16, +1, E, Lin>(w);
+#pragma unroll
+            for (int q = 0; q < QB; ++q) tws[(QB + 2 + q) * NT + t] = w[q];
+        }
+        if (!LEAN) {
+#pragma unroll
+            for (int q = 0; q < QL; ++q) {
+                int seq, j;
+                Lin::at<L, RL>(q, seq, j);
+                tws[(2 * QB + 2 + q) * NT + t] = unit_root<+1>(j % NSL, NSL * RL);
             }
         }
+    }
+    // Tile tl -> sm.  TMA: L/BOXR boxes land row-major, sm[m1 * CPT + c], and complete on `bar`
+    // (caller: all threads past their last generic access to sm and a proxy fence).  Otherwise 8-byte
+    // asynchronous copies into the padded column layout sm[c * SP + pad(m1)].  The row segments of
+    // neighbouring tiles share sectors, so both forms read through L2 normally.
+    auto load_tile = [&](int tl) {
+        if (tl >= ntiles) return;
+        if (TMA) {
+            if (t == 0) {
+                mbar_expect_tx(&bar, (uint32_t)(CPT * L * sizeof(float2)));
+#pragma unroll 1
+                for (int b = 0; b < L / BOXR; ++b)
+                    tma_load_2d(sm + b * BOXR * CPT, &mapY, 2 * CPT * tl, BOXR * b, &bar);
+            }
+        } else {
+#pragma unroll 4
+            for (int i = 0; i < L * CPT / 2 / NT; ++i) {
+                const int idx = t + i * NT, m1 = idx / (CPT / 2), cp = idx % (CPT / 2);
+                const float2* src = Y + (size_t)m1 * n2 + (size_t)tl * CPT + 2 * cp;
+                cp_async8(sm + (2 * cp) * SP + padk<4>(m1), src);
+                cp_async8(sm + (2 * cp + 1) * SP + padk<4>(m1), src + 1);
+            }
+        }
+    };
+    uint32_t parity = 0;
+    auto wait_tile = [&]() {
+        if (TMA) {
+            if (!s_fail && !mbar_wait(&bar, parity)) {
+                s_fail = 1;
+                atomicExch(err, kErrTmaTimeout);
+            }
+            parity ^= 1u;
+        } else {
+            cp_async_wait_all();
+        }
+    };
+    if (t == 0) {
+        s_fail = 0;
+        mbar_init(&bar, 1);
+    }
+    __syncthreads();
+    // The last inverse stage writes straight from registers when the linear map gives each thread both
+    // columns of a pair for the same rows; the tile buffer is then free during that stage and the next
+    // tile's copies overlap with it.
+    constexpr bool DIRECT = CPT == 2 && NSL == NT && QL == 2;
+    fence_proxy_async();
+    load_tile(blockIdx.x);
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        // the tile's seed spectrum (contiguous) is read after the forward FFT: start it into L2 now
+        if (!SEED && t == 0)
+            prefetch_l2(spec + (size_t)tile * (CPT * L), CPT * L * sizeof(float2));
+        if (!DIRECT || SEED) {
+            if (tile != (int)blockIdx.x) {
+                __syncthreads();  // previous tile done with sm
+                fence_proxy_async();
+                load_tile(tile);
+            }
+        }
+        wait_tile();
+        __syncthreads();  // tile copies visible; previous tile done with the tables
         if (!SEED) {
-            for (int i = t; i < CPT * RL; i += NT) {
-                int c = i / RL, r = i % RL;
-                uint32_t k2 = col_k2((uint32_t)tile * (CPT / 2) + (uint32_t)(c >> 1), c & 1, n2);
-                uint64_t e = ((uint64_t)(L / RL) * (uint64_t)r * k2) & ((1ull << g.log_n) - 1);
-                sigma[i] = cconj(expmi_pi((uint32_t)(2 * e), g.log_n));
+            for (int i = t; i < CPT * (RL + U1N + U2N); i += NT) {
+                int c, kind, r;
+                if (i < CPT * RL) { c = i / RL; r = i % RL; kind = 0; }
+                else if (i < CPT * (RL + U1N)) { c = (i - CPT * RL) / U1D; r = (i - CPT * RL) % U1D; kind = 1; }
+                else { c = (i - CPT * (RL + U1N)) / U2D; r = (i - CPT * (RL + U1N)) % U2D; kind = 2; }
+                uint64_t k2 = col_k2((uint32_t)tile * (CPT / 2) + (uint32_t)(c >> 1), c & 1, n2);
+                uint64_t mult = kind == 0 ? (uint64_t)NSL * r : (kind == 1 ? (uint64_t)r : (uint64_t)U1N * r);
+                uint64_t e = (mult * k2) & ((1ull << g.log_n) - 1);
+                float2 w = expmi_pi((uint32_t)(2 * e), g.log_n);
+                if (kind == 0) sigma[c * RL + r] = cconj(w);
+                else if (kind == 1) u1[c * U1N + r] = w;
+                else u2[c * U2N + r] = w;
             }
         }
         __syncthreads();
         float2 x[E];
-        gather_inputs<L, E, P::RA, Lin>(x, sm);
-        stage<L, P::RA, 1, -1, E, Lin>(x);
-        if (P::NSTAGE == 2) {
-            exchange<L, E, P::RA, 1, Lin, P::RB, Lin>(x, sm);
-            stage<L, P::RB, P::RA, -1, E, Lin>(x);
-            exchange<L, E, P::RB, P::RA, Lin, 16, MapMirrorPair>(x, sm);
+        if (TMA) {  // row-major tile: element m1 of column c at sm[m1 * CPT + c]
+#pragma unroll
+            for (int q = 0; q < E / P::RA; ++q) {
+                int seq, j;
+                Lin::at<L, P::RA>(q, seq, j);
+#pragma unroll
+                for (int r = 0; r < P::RA; ++r) x[q * P::RA + r] = sm[(j + r * (L / P::RA)) * CPT + seq];
+            }
         } else {
-            exchange<L, E, P::RA, 1, Lin, 16, MapMirrorPair>(x, sm);
+            gather_inputs<L, SP, E, P::RA, Lin>(x, sm);
         }
-        stage<L, 16, LR, -1, E, MapMirrorPair>(x);
+        stage<P::RA, 1, -1, E>(x, nullptr);
+        if (P::NSTAGE == 2) {
+            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm);
+            float2 w[QB > 0 ? QB : 1];
+#pragma unroll
+            for (int q = 0; q < QB; ++q) w[q] = tws[q * NT + t];
+            stage<P::RB, P::RA, -1, E>(x, w);
+            exchange<L, SP, 4, E, P::RB, P::RA, Lin, 16, MapMirrorPair>(x, sm);
+        } else {
+            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorPair>(x, sm);
+        }
+        {
+            float2 w[2] = {tws[QB * NT + t], tws[(QB + 1) * NT + t]};
+            stage<16, LR, -1, E>(x, w);
+        }
 
         // ---- spectral step: real split, product with the seed spectrum, real merge
         float2* tspec = spec + (size_t)tile * (CPT * L);
@@ -257,8 +429,9 @@ __global__ void __launch_bounds__(512, 1)
                 for (int q = 0; q < 2; ++q) {
                     int seq, j;
                     MapMirrorPair::at<L, 16>(q, seq, j);
+                    float2* b = sm + seq * SP + padk<4>(j);
 #pragma unroll
-                    for (int r = 0; r < 16; ++r) sm[seq * SP + pad16(j + LR * r)] = x[16 * q + r];
+                    for (int r = 0; r < 16; ++r) b[padoff<4>(LR * r)] = x[16 * q + r];
                 }
             }
             __syncthreads();
@@ -278,19 +451,19 @@ __global__ void __launch_bounds__(512, 1)
                         k = n2 / 2 + n2 * (uint32_t)ka;
                     }
                     if (u == 0) {  // DC (dropped) and Nyquist in slot (0, 0); then the self pair N/2
-                        float2 z = sm[pad16(0)];
+                        float2 z = sm[padk<4>(0)];
                         float nyq = 2.0f * (z.x - z.y);
                         if (SEED) {
                             tspec[spec_index<LR>(0, 0)] = make_float2(nyq * sc, 0.f);
                         } else {
                             float pn = nyq * tspec[spec_index<LR>(0, 0)].x;
-                            sm[pad16(0)] = make_float2(pn, -pn);
+                            sm[padk<4>(0)] = make_float2(pn, -pn);
                         }
                         ka = kb = L / 2;
                         k = n2 * (uint32_t)(L / 2);
                     }
                     float2 w = expmi_pi(k, g.log_n);
-                    float2 za = sm[ca * SP + pad16(ka)], zb = sm[cb * SP + pad16(kb)];
+                    float2 za = sm[ca * SP + padk<4>(ka)], zb = sm[cb * SP + padk<4>(kb)];
                     float2 xa, xb;
                     real_split(za, zb, w, xa, xb);
                     int ia = spec_index<LR>(ca, ka), ib = spec_index<LR>(cb, kb);
@@ -300,8 +473,8 @@ __global__ void __launch_bounds__(512, 1)
                     } else {
                         float2 qa, qb;
                         real_merge(cmul(xa, tspec[ia]), cmul(xb, tspec[ib]), w, qa, qb);
-                        sm[ca * SP + pad16(ka)] = qa;
-                        sm[cb * SP + pad16(kb)] = qb;
+                        sm[ca * SP + padk<4>(ka)] = qa;
+                        sm[cb * SP + padk<4>(kb)] = qb;
                     }
                 }
             }
@@ -311,8 +484,9 @@ __global__ void __launch_bounds__(512, 1)
                 for (int q = 0; q < 2; ++q) {
                     int seq, j;
                     MapMirrorPair::at<L, 16>(q, seq, j);
+                    const float2* b = sm + seq * SP + padk<4>(j);
 #pragma unroll
-                    for (int r = 0; r < 16; ++r) x[16 * q + r] = sm[seq * SP + pad16(j + LR * r)];
+                    for (int r = 0; r < 16; ++r) x[16 * q + r] = b[padoff<4>(LR * r)];
                 }
             }
         }
@@ -321,20 +495,22 @@ __global__ void __launch_bounds__(512, 1)
             // W_2N^{p + N2 (jj + LR r)} = W_2N^{p + N2 jj} * W_32^r
             const uint32_t p = (uint32_t)tile * (CPT / 2) + (uint32_t)pp;
             const float2 base = expmi_pi(p + n2 * (uint32_t)jj, g.log_n);
-            const int ia0 = (2 * pp) * 16 * LR + jj, ib0 = (2 * pp + 1) * 16 * LR + jj;
+            const float2* sa = tspec + (2 * pp) * 16 * LR + jj;
+            const float2* sb = tspec + (2 * pp + 1) * 16 * LR + jj;
+            float2* da = reinterpret_cast<float2*>(const_cast<float2*>(sa));
+            float2* db = reinterpret_cast<float2*>(const_cast<float2*>(sb));
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
                 // W_32^r = e^{-i pi r/16} = (cos, -sin)(2 pi r/32), r < 16
                 const float2 w = r ? cmul(base, make_float2(w32(r).x, -w32(r).y)) : base;
                 float2 xa, xb;
                 real_split(x[r], x[16 + 15 - r], w, xa, xb);
-                const int ia = ia0 + r * LR, ib = ib0 + (15 - r) * LR;
                 if (SEED) {
-                    __stcs(tspec + ia, cscale(xa, sc));
-                    __stcs(tspec + ib, cscale(xb, sc));
+                    __stcs(da + r * LR, cscale(xa, sc));
+                    __stcs(db + (15 - r) * LR, cscale(xb, sc));
                 } else {
                     float2 qa, qb;
-                    real_merge(cmul(xa, __ldcs(tspec + ia)), cmul(xb, __ldcs(tspec + ib)), w, qa, qb);
+                    real_merge(cmul(xa, __ldcs(sa + r * LR)), cmul(xb, __ldcs(sb + (15 - r) * LR)), w, qa, qb);
                     x[r] = qa;
                     x[16 + 15 - r] = qb;
                 }
@@ -343,81 +519,158 @@ __global__ void __launch_bounds__(512, 1)
         if (SEED) continue;
 
         // ---- inverse column FFTs (radices 16, RB, RA) with the inverse 4-step twiddle folded into
-        // the last stage: conj(W_N^{m1 k2}), m1 = j + (L/RL) r
-        stage<L, 16, 1, +1, E, MapMirrorPair>(x);
+        // the last stage: conj(W_N^{m1 k2}), m1 = j + NSL r
+        stage<16, 1, +1, E>(x, nullptr);
         if (P::NSTAGE == 2) {
-            exchange<L, E, 16, 1, MapMirrorPair, P::RB, Lin>(x, sm);
-            stage<L, P::RB, 16, +1, E, Lin>(x);
-            exchange<L, E, P::RB, 16, Lin, P::RA, Lin>(x, sm);
-        } else {
-            exchange<L, E, 16, 1, MapMirrorPair, P::RA, Lin>(x, sm);
-        }
-        constexpr int NSL = L / RL;
+            exchange<L, SP, 4, E, 16, 1, MapMirrorPair, P::RB, Lin>(x, sm);
+            float2 w[QB > 0 ? QB : 1];
 #pragma unroll
-        for (int q = 0; q < E / RL; ++q) {
+            for (int q = 0; q < QB; ++q) w[q] = tws[(QB + 2 + q) * NT + t];
+            stage<P::RB, 16, +1, E>(x, w);
+            exchange<L, SP, 4, E, P::RB, 16, Lin, RL, Lin>(x, sm);
+        } else {
+            exchange<L, SP, 4, E, 16, 1, MapMirrorPair, RL, Lin>(x, sm);
+        }
+        if (DIRECT) {  // after the last exchange sm is free until the next tile
+            __syncthreads();
+            fence_proxy_async();
+            load_tile(tile + gridDim.x);
+        }
+#pragma unroll
+        for (int q = 0; q < QL; ++q) {
             int seq, j;
             Lin::at<L, RL>(q, seq, j);
-            uint32_t k2 = col_k2((uint32_t)tile * (CPT / 2) + (uint32_t)(seq >> 1), seq & 1, n2);
-            uint64_t e = ((uint64_t)j * k2) & ((1ull << g.log_n) - 1);
-            float2 c = cconj(expmi_pi((uint32_t)(2 * e), g.log_n));
-            if (NSL > 1) twiddle_powers<RL, true>(&x[q * RL], unit_root<+1>(j % NSL, NSL * RL), c);
-            else {
-#pragma unroll
-                for (int r = 0; r < RL; ++r) x[q * RL + r] = cmul(x[q * RL + r], c);
+            float2 c, wbase;
+            if (LEAN) {
+                uint32_t k2 = col_k2((uint32_t)tile * (CPT / 2) + (uint32_t)(seq >> 1), seq & 1, n2);
+                c = cconj(expmi_pi((uint32_t)((2ull * j * k2) & ((2ull << g.log_n) - 1)), g.log_n));
+                wbase = unit_root<+1>(j % NSL, NSL * RL);
+            } else {
+                c = cconj(cmul(u1[seq * U1N + j % U1D], u2[seq * U2N + j / U1D]));
+                wbase = tws[(2 * QB + 2 + q) * NT + t];
             }
+            twiddle_powers<RL, true>(&x[q * RL], wbase, c);
             dft<RL, +1>(reinterpret_cast<float2(&)[RL]>(x[q * RL]));
 #pragma unroll
             for (int r = 0; r < RL; ++r) x[q * RL + r] = cmul(x[q * RL + r], sigma[seq * RL + r]);
         }
+        float4* Z4 = reinterpret_cast<float4*>(Z) + (size_t)tile * L * (CPT / 2);  // this tile, [m1][CPT/2]
+        if (DIRECT) {  // thread holds column 0 (x[0..RL)) and column 1 (x[RL..2RL)) of rows j + NSL r
+#pragma unroll
+            for (int r = 0; r < RL; ++r)
+                __stcg(Z4 + t + NSL * r, make_float4(x[r].x, x[r].y, x[RL + r].x, x[RL + r].y));
+            continue;
+        }
         __syncthreads();
-        scatter_outputs<L, E, RL, Lin>(x, sm);
+        scatter_outputs<L, SP, E, RL, Lin>(x, sm);
         __syncthreads();
-        {
-            float4* Y4 = reinterpret_cast<float4*>(Y);
-            for (int idx = t; idx < L * CPT / 2; idx += NT) {
-                int m1 = idx / (CPT / 2), cp = idx % (CPT / 2);
-                float2 a = sm[(2 * cp) * SP + pad16(m1)], b = sm[(2 * cp + 1) * SP + pad16(m1)];
-                __stcg(Y4 + (((size_t)m1 * n2 + (size_t)tile * CPT) >> 1) + cp, make_float4(a.x, a.y, b.x, b.y));
-            }
+#pragma unroll 4
+        for (int i = 0; i < L * CPT / 2 / NT; ++i) {
+            int idx = t + i * NT, m1 = idx / (CPT / 2), cp = idx % (CPT / 2);
+            float2 a = sm[(2 * cp) * SP + padk<4>(m1)], b = sm[(2 * cp + 1) * SP + padk<4>(m1)];
+            __stcg(Z4 + idx, make_float4(a.x, a.y, b.x, b.y));
         }
     }
 }
 
 // ============================================================================ pass C
 // Row m1: inverse FFT over k2 (radices 16, RB, RA), + correction, round, parity bit planes.
+// Input: Z, tile-major from pass B.  Row m1 is the CPT/2 pairs of row m1 of every tile; 3D TMA boxes
+// (256 tiles x 1 row x CPT/2 pairs) gather it into shared memory in pair order (float4 p = pair p),
+// or cooperative loads when a tile row is too wide for a box.  The next row's copy starts as soon as
+// the last exchange of the current row has finished with the buffer.
 template <int LOGL>
 __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
-    k_pass_c(const float2* __restrict__ Y, BlockGeom g, const unsigned long long* cnt,
-             uint32_t* __restrict__ planes, unsigned int* resid_bits) {
-    constexpr int L = 1 << LOGL, NT = L / 32, E = 32, LR = L / 16;
+    k_pass_c(const __grid_constant__ CUtensorMap mapZ, const float2* __restrict__ Z, BlockGeom g,
+             const unsigned long long* cnt, uint32_t* __restrict__ planes, unsigned int* resid_bits, int* err) {
+    constexpr int L = 1 << LOGL, NT = L / 32, E = 32, LR = L / 16, SP = TileStride<L>::value;
     using P = Plan<LOGL>;
     using Lin = MapLinear<NT>;
     constexpr int RL = P::RA, NSL = L / RL;
-    extern __shared__ float2 sm[];
+    constexpr int QB = P::NSTAGE == 2 ? E / P::RB : 0;
+    constexpr int QL = E / RL;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float2* sm = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    __shared__ float2 tws[(QB > 0 ? QB : 1) + QL][NT];
     __shared__ float redf[32];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_fail;
     const uint32_t n1 = 1u << g.log_n1;
+    const int cpt = 8192 >> g.log_n1;               // pass B tile width (columns)
+    const int pairs_per_tile = cpt / 2;
+    const int ntiles = (int)(L / cpt);
+    const bool tma = cpt <= 128;
+    const int boxt = ntiles < 256 ? ntiles : 256;   // tiles per box
     const int t = threadIdx.x, lane = t & 31;
+    {
+        float2 w[4];
+        if (P::NSTAGE == 2) {
+            stage_bases<L, P::RB, 16, +1, E, Lin>(w);
+#pragma unroll
+            for (int q = 0; q < QB; ++q) tws[q][t] = w[q];
+            stage_bases<L, RL, 16 * P::RB, +1, E, Lin>(w);
+        } else {
+            stage_bases<L, RL, 16, +1, E, Lin>(w);
+        }
+#pragma unroll
+        for (int q = 0; q < QL; ++q) tws[(QB > 0 ? QB : 1) + q][t] = w[q];
+    }
     float corr;
     {
         unsigned long long ck = cnt[0], cs = cnt[1];
         unsigned long long pm = (ck * cs) & ((2ull << g.log_np) - 1ull);
         corr = (float)((double)pm / (double)(1ull << g.log_np));
     }
+    // rows holding at least one output sample: m1 < min(N1, ceil(out_bits / 2))
+    const uint32_t rows_out = (uint32_t)(((uint64_t)g.out_bits + 1ull) / 2ull < n1 ? (g.out_bits + 1u) / 2u : n1);
+    auto load_row = [&](uint32_t r) {
+        if (r >= rows_out) return;
+        if (tma) {
+            if (t == 0) {
+                mbar_expect_tx(&bar, (uint32_t)(L * sizeof(float2)));
+#pragma unroll 1
+                for (int b = 0; b < ntiles / boxt; ++b)
+                    tma_load_3d(sm + (size_t)b * boxt * cpt, &mapZ, 0, (int)r, boxt * b, &bar);
+            }
+        } else {
+            const float4* z4 = reinterpret_cast<const float4*>(Z);
+            float4* s4 = reinterpret_cast<float4*>(sm);
+            for (int p = t; p < L / 2; p += NT) {
+                int tl = p / pairs_per_tile, cp = p % pairs_per_tile;
+                s4[p] = __ldcs(z4 + ((size_t)tl * n1 + r) * pairs_per_tile + cp);
+            }
+        }
+    };
+    uint32_t parity = 0;
+    if (t == 0) {
+        s_fail = 0;
+        mbar_init(&bar, 1);
+    }
+    __syncthreads();
     const size_t plane_words = (size_t)n1 * (L / 32);
+    // rows without output samples: zero planes
+    for (uint32_t m1 = rows_out + blockIdx.x; m1 < n1; m1 += gridDim.x)
+        for (int w = t; w < L / 32; w += NT) planes[(size_t)m1 * (L / 32) + w] = planes[plane_words + (size_t)m1 * (L / 32) + w] = 0u;
+    fence_proxy_async();
+    load_row(blockIdx.x);
     float res = 0.f;
-    for (uint32_t m1 = blockIdx.x; m1 < n1; m1 += gridDim.x) {
+    for (uint32_t m1 = blockIdx.x; m1 < rows_out; m1 += gridDim.x) {
         uint32_t* pe = planes + (size_t)m1 * (L / 32);
         uint32_t* po = pe + plane_words;
-        if (2ull * m1 >= g.out_bits) {  // no output sample in this row
-            for (int w = t; w < L / 32; w += NT) pe[w] = po[w] = 0u;
-            continue;
+        if (tma) {
+            if (!s_fail && !mbar_wait(&bar, parity)) {
+                s_fail = 1;
+                atomicExch(err, kErrTmaTimeout);
+            }
+            parity ^= 1u;
         }
+        __syncthreads();  // row in sm
         float2 x[E];
-        const float4* row4 = reinterpret_cast<const float4*>(Y + ((size_t)m1 << LOGL));
+        const float4* row4 = reinterpret_cast<const float4*>(sm);
         if (t != 0) {
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
-                float4 a = __ldcs(row4 + t + LR * r), b = __ldcs(row4 + (LR - t) + LR * r);
+                float4 a = row4[t + LR * r], b = row4[(LR - t) + LR * r];
                 x[r] = make_float2(a.x, a.y);
                 x[16 + 15 - r] = make_float2(a.z, a.w);
                 x[16 + r] = make_float2(b.x, b.y);
@@ -426,26 +679,36 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
         } else {
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
-                float4 a = __ldcs(row4 + LR * r), b = __ldcs(row4 + LR / 2 + LR * r);
+                float4 a = row4[LR * r], b = row4[LR / 2 + LR * r];
                 x[r] = make_float2(a.x, a.y);
                 x[r == 0 ? 8 : 16 - r] = make_float2(a.z, a.w);
                 x[16 + r] = make_float2(b.x, b.y);
                 x[16 + 15 - r] = make_float2(b.z, b.w);
             }
         }
-        stage<L, 16, 1, +1, E, MapMirrorRow>(x);
-        if (P::NSTAGE == 2) {
-            exchange<L, E, 16, 1, MapMirrorRow, P::RB, Lin>(x, sm);
-            stage<L, P::RB, 16, +1, E, Lin>(x);
-            exchange<L, E, P::RB, 16, Lin, RL, Lin>(x, sm);
-            stage<L, RL, 16 * P::RB, +1, E, Lin>(x);
-        } else {
-            exchange<L, E, 16, 1, MapMirrorRow, RL, Lin>(x, sm);
-            stage<L, RL, 16, +1, E, Lin>(x);
+        stage<16, 1, +1, E>(x, nullptr);
+        {
+            float2 w[4];
+            if (P::NSTAGE == 2) {
+                exchange<L, SP, 4, E, 16, 1, MapMirrorRow, P::RB, Lin>(x, sm);
+#pragma unroll
+                for (int q = 0; q < QB; ++q) w[q] = tws[q][t];
+                stage<P::RB, 16, +1, E>(x, w);
+                exchange<L, SP, 4, E, P::RB, 16, Lin, RL, Lin>(x, sm);
+            } else {
+                exchange<L, SP, 4, E, 16, 1, MapMirrorRow, RL, Lin>(x, sm);
+            }
+            // sm is free: start the next row's copy under the last stage
+            __syncthreads();
+            fence_proxy_async();
+            load_row(m1 + gridDim.x);
+#pragma unroll
+            for (int q = 0; q < QL; ++q) w[q] = tws[(QB > 0 ? QB : 1) + q][t];
+            stage<RL, (P::NSTAGE == 2 ? 16 * P::RB : 16), +1, E>(x, w);
         }
         // outputs: butterfly u = t + q*NT (j = u), sample m2 = j + NSL*r; lanes hold consecutive m2
 #pragma unroll
-        for (int q = 0; q < E / RL; ++q) {
+        for (int q = 0; q < QL; ++q) {
             const int j = t + q * NT;
 #pragma unroll
             for (int r = 0; r < RL; ++r) {
@@ -465,16 +728,18 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
                 }
             }
         }
-        __syncthreads();  // exchanges of the next row reuse sm
+        if (!tma) __syncthreads();  // cooperative loads of the next row happen at the top
     }
     float bm = block_max_f(res, redf);
     if (threadIdx.x == 0) atomicMax(resid_bits, __float_as_uint(bm));
 }
 
 // ============================================================================ finish
-// Warp (a, c): plane rows m1 = 32a .. 32a+31 (lane), plane word column c (m2 = 32c .. 32c+31).
-// Output word ow = (m2 N1 + m1_0)/16 holds samples m1_0 .. m1_0+15 of column m2, bits (even, odd)
-// interleaved in the reference byte order; XOR with key_rest word ow.
+// Warp (a, c): plane rows m1 = 32a + lane, plane word column c (m2 = 32c .. 32c+31).  Each lane packs
+// its (even, odd) parities of 16 columns into 2-bit elements and a half-warp transpose turns them into
+// output words: lane L of half h holds column 32c + L (+16 for the second word), samples
+// m1 = 32a + 16h .. +15 -- output word ow = (m2 N1 + 32a + 16h)/16, bits in the reference byte order,
+// XORed with key_rest word ow.
 __global__ void __launch_bounds__(1024) k_finish(const uint32_t* __restrict__ planes, BlockGeom g,
                                                  const uint32_t* __restrict__ key_rest, uint32_t flags,
                                                  uint32_t* __restrict__ out, uint32_t nwords) {
@@ -486,23 +751,15 @@ __global__ void __launch_bounds__(1024) k_finish(const uint32_t* __restrict__ pl
     if (a >= n1 / 32u || c >= wpr) return;
     const size_t off = (size_t)(32u * a + (uint32_t)lane) * wpr + c;
     const uint32_t ve = __ldg(planes + off), vo = __ldg(planes + plane_words + off);
-    uint32_t e_lo = 0, o_lo = 0;
+    const uint32_t lo = transpose16x2(msb_pairs(ve, vo), lane);
+    const uint32_t hi = transpose16x2(msb_pairs(ve >> 16, vo >> 16), lane);
+    const uint32_t L = (uint32_t)(lane & 15), h = (uint32_t)(lane >> 4);
 #pragma unroll
-    for (int b = 0; b < 32; ++b) {
-        uint32_t e = __ballot_sync(0xffffffffu, (ve >> b) & 1u);
-        uint32_t o = __ballot_sync(0xffffffffu, (vo >> b) & 1u);
-        if (lane == b) {
-            e_lo = e;
-            o_lo = o;
-        }
-    }
-    const uint32_t m2 = 32u * c + (uint32_t)lane;
-    const uint64_t ow0 = ((uint64_t)m2 * n1 + 32ull * a) / 16ull;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const uint64_t ow = ow0 + (uint64_t)h;
+    for (int k = 0; k < 2; ++k) {
+        const uint64_t m2 = 32ull * c + L + 16u * k;
+        const uint64_t ow = (m2 * n1 + 32ull * a + 16ull * h) / 16ull;
         if (ow >= nwords) continue;
-        uint32_t w = msb_pairs(h ? e_lo >> 16 : e_lo, h ? o_lo >> 16 : o_lo);
+        uint32_t w = k ? hi : lo;
         if ((flags & kXor) && 32ull * ow < g.v) w ^= __ldg(key_rest + ow);
         out[ow] = __byte_perm(w, 0, 0x0123);
     }
@@ -530,7 +787,7 @@ template <int LOGL>
 static int pass_a_l(const BlockGeom& g, const uint32_t* rows, bool seed, float2* Y, unsigned long long* cnt,
                     int num_sms, cudaStream_t s) {
     constexpr int NT = (1 << LOGL) / 32;
-    size_t smem = (size_t)Padded<(1 << LOGL)>::value * sizeof(float2);
+    size_t smem = (size_t)TileStride<(1 << LOGL)>::value * sizeof(float2);
     int grid = grid_units(1u << g.log_n1, num_sms);
     if (seed) {
         smem_attr(k_pass_a<LOGL, true>, smem);
@@ -543,27 +800,34 @@ static int pass_a_l(const BlockGeom& g, const uint32_t* rows, bool seed, float2*
 }
 
 template <int LOGL>
-static int pass_b_l(const BlockGeom& g, bool seed, float2* Y, float2* spec, int num_sms, cudaStream_t s) {
-    constexpr int L = 1 << LOGL, CPT = 16384 / L;
-    size_t smem = ((size_t)CPT * Padded<L>::value + (size_t)CPT * Plan<LOGL>::RA) * sizeof(float2);
-    int grid = grid_units((1u << g.log_n2) / CPT, num_sms);
+static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y, float2* Z, float2* spec,
+                    int* err, int num_sms, cudaStream_t s) {
+    constexpr int L = 1 << LOGL, CPT = 8192 / L, RL = Plan<LOGL>::RA, NSL = L / RL;
+    constexpr bool LEAN = LOGL <= 6;
+    constexpr int U1N = LEAN ? 0 : (NSL < 16 ? NSL : 16), U2N = LEAN ? 0 : NSL / U1N;
+    constexpr int QB = Plan<LOGL>::NSTAGE == 2 ? 32 / Plan<LOGL>::RB : 0, QL = LEAN ? 0 : 32 / RL;
+    constexpr size_t words = (size_t)CPT * TileStride<L>::value + (size_t)CPT * (RL + U1N + U2N) +
+                             (size_t)(2 * QB + 2 + QL) * 256;
+    static_assert(words * sizeof(float2) + 128 <= 112 * 1024, "pass B tile too large for two CTAs per SM");
+    size_t smem = words * sizeof(float2) + 128;  // + alignment of the TMA destination
+    int grid = grid_units((1u << g.log_n2) / CPT, 2 * num_sms);
     if (seed) {
         smem_attr(k_pass_b<LOGL, true>, smem);
-        k_pass_b<LOGL, true><<<grid, 512, smem, s>>>(Y, g, spec);
+        k_pass_b<LOGL, true><<<grid, 256, smem, s>>>(maps.y, Y, Z, g, spec, err);
     } else {
         smem_attr(k_pass_b<LOGL, false>, smem);
-        k_pass_b<LOGL, false><<<grid, 512, smem, s>>>(Y, g, spec);
+        k_pass_b<LOGL, false><<<grid, 256, smem, s>>>(maps.y, Y, Z, g, spec, err);
     }
     return (int)cudaGetLastError();
 }
 
 template <int LOGL>
-static int pass_c_l(const BlockGeom& g, const float2* Y, const unsigned long long* cnt, uint32_t* planes,
-                    unsigned int* resid, int num_sms, cudaStream_t s) {
+static int pass_c_l(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
+                    uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s) {
     constexpr int NT = (1 << LOGL) / 32;
-    size_t smem = (size_t)Padded<(1 << LOGL)>::value * sizeof(float2);
+    size_t smem = (size_t)TileStride<(1 << LOGL)>::value * sizeof(float2) + 128;  // + TMA alignment
     smem_attr(k_pass_c<LOGL>, smem);
-    k_pass_c<LOGL><<<grid_units(1u << g.log_n1, num_sms), NT, smem, s>>>(Y, g, cnt, planes, resid);
+    k_pass_c<LOGL><<<grid_units(1u << g.log_n1, num_sms), NT, smem, s>>>(maps.z, Z, g, cnt, planes, resid, err);
     return (int)cudaGetLastError();
 }
 
@@ -596,17 +860,59 @@ int launch_pass_a(const BlockGeom& g, const uint32_t* rows, bool seed, float2* Y
 #undef C
 }
 
-int launch_pass_b(const BlockGeom& g, bool seed, float2* Y, float2* spec, int num_sms, cudaStream_t s) {
-#define C(LG) pass_b_l<LG>(g, seed, Y, spec, num_sms, s)
+int launch_pass_b(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y, float2* Z, float2* spec, int* err,
+                  int num_sms, cudaStream_t s) {
+#define C(LG) pass_b_l<LG>(g, seed, maps, Y, Z, spec, err, num_sms, s)
     PA_COLS_DISPATCH(g.log_n1, C)
 #undef C
 }
 
-int launch_pass_c(const BlockGeom& g, const float2* Y, const unsigned long long* cnt, uint32_t* planes,
-                  unsigned int* resid, int num_sms, cudaStream_t s) {
-#define C(LG) pass_c_l<LG>(g, Y, cnt, planes, resid, num_sms, s)
+int launch_pass_c(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
+                  uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s) {
+#define C(LG) pass_c_l<LG>(g, maps, Z, cnt, planes, resid, err, num_sms, s)
     PA_ROWS_DISPATCH(g.log_n2, C)
 #undef C
+}
+
+// Tensor maps of the two strided transfers (see k_pass_b / k_pass_c).  cuTensorMapEncodeTiled is taken
+// from the driver through the runtime, so the library does not link libcuda.
+int make_pass_maps(const BlockGeom& g, const float2* Y, const float2* Z, PassMaps* out) {
+    std::memset(out, 0, sizeof(*out));
+    if (g.log_n1 == 0) return 0;
+    const uint64_t n1 = 1ull << g.log_n1, n2 = 1ull << g.log_n2;
+    const uint64_t cpt = 8192ull >> g.log_n1;
+    if (cpt > 128) return 0;  // transfers use per-thread copies instead
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return (int)cudaErrorNotSupported;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint32_t estr[3] = {1, 1, 1};
+    {   // Y: rows of 2 N2 floats; box = 2 CPT floats x min(N1, 256) rows
+        const cuuint64_t dims[2] = {2 * n2, n1};
+        const cuuint64_t strides[1] = {2 * n2 * sizeof(float)};
+        const cuuint32_t box[2] = {(cuuint32_t)(2 * cpt), (cuuint32_t)(n1 < 256 ? n1 : 256)};
+        CUresult r = encode(&out->y, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(Y), dims, strides, box,
+                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return (int)cudaErrorInvalidValue;
+    }
+    {   // Z: [tile][m1][2 CPT floats]; box = 2 CPT floats x 1 row x min(ntiles, 256) tiles
+        const uint64_t ntiles = n2 / cpt;
+        const cuuint64_t dims[3] = {2 * cpt, n1, ntiles};
+        const cuuint64_t strides[2] = {2 * cpt * sizeof(float), n1 * 2 * cpt * sizeof(float)};
+        const cuuint32_t box[3] = {(cuuint32_t)(2 * cpt), 1, (cuuint32_t)(ntiles < 256 ? ntiles : 256)};
+        CUresult r = encode(&out->z, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(Z), dims, strides, box,
+                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return (int)cudaErrorInvalidValue;
+    }
+    return 0;
 }
 
 int launch_finish(const BlockGeom& g, const uint32_t* planes, const uint32_t* key_rest, uint32_t flags,

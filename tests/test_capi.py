@@ -37,7 +37,7 @@ def test_output_bytes():
 
 def test_kernels_per_block():
     assert pa.kernels_per_block(2048, 1024, 0) == 1
-    assert pa.kernels_per_block(1 << 27, 50331648) == 4
+    assert pa.kernels_per_block(1 << 27, 50331648) == 5  # bit rows, passes A, B, C, finish
     assert pa.kernels_per_block(1000, 96) == 0  # rejected size
 
 
