@@ -45,6 +45,16 @@ static inline uint32_t bit_msb(const uint32_t *w, uint64_t i) {
     return (w[i >> 5] >> (31u - (uint32_t)(i & 31u))) & 1u;
 }
 
+static inline uint32_t brev32(uint32_t x) {
+    x = ((x >> 1) & 0x55555555u) | ((x & 0x55555555u) << 1);
+    x = ((x >> 2) & 0x33333333u) | ((x & 0x33333333u) << 2);
+    x = ((x >> 4) & 0x0F0F0F0Fu) | ((x & 0x0F0F0F0Fu) << 4);
+    x = ((x >> 8) & 0x00FF00FFu) | ((x & 0x00FF00FFu) << 8);
+    return (x >> 16) | (x << 16);
+}
+
+static inline uint64_t brev64(uint64_t x) { return ((uint64_t)brev32((uint32_t)x) << 32) | brev32((uint32_t)(x >> 32)); }
+
 /* key2StartRest (PrivacyAmplification.cu:861-892): key_start = key words 0..h/32-1 plus the top bit of
  * word h/32 (h+1 bits); key_rest = key bits h+1 .. h+v realigned by a 1-bit left shift.
  * recv_key holds n/32+1 words.  key_start receives n/32 words (zero past h/32), key_rest v/32 words. */
@@ -96,12 +106,33 @@ void *pa_oracle_direct_prepare(const uint32_t *seed, const uint32_t *key_start, 
     uint64_t rw = (rbits + 63u) / 64u + 1u;
     c->K = (uint64_t *)calloc(c->kw, 8);
     c->R = (uint64_t *)calloc(rw, 8);
-    for (uint64_t j = 0; j <= c->h; ++j)
-        if (bit_msb(key_start, j)) c->K[j >> 6] |= 1ull << (j & 63);
-    for (uint64_t m = 0; m < rbits; ++m) {
-        uint64_t src = (n - (m % n)) % n;
-        if (bit_msb(seed, src)) c->R[m >> 6] |= 1ull << (m & 63);
+    /* K: key bits 0..h, LSB-first 64-bit words (bit-reversal of the MSB-first 32-bit words) */
+    for (uint64_t w = 0; w <= c->h / 32; ++w) {
+        uint64_t b = brev32(key_start[w]);
+        c->K[w >> 1] |= b << (32 * (w & 1));
     }
+    if ((c->h + 1) % 64) c->K[c->kw - 1] &= ~0ull >> (64 - (c->h + 1) % 64);
+    /* S: seed, LSB-first; R[m] = S[(n - m) mod n], periodically extended: 64 bits of R at m0 are the
+     * bit-reversed window S[a .. a+63] with a = n - m0 - 63 (taken mod n, bit by bit only on a wrap) */
+    uint64_t sw = ((uint64_t)n + 63) / 64 + 1;
+    uint64_t *S = (uint64_t *)calloc(sw, 8);
+    for (uint64_t w = 0; w < n / 32; ++w) S[w >> 1] |= (uint64_t)brev32(seed[w]) << (32 * (w & 1));
+    for (uint64_t k = 0; k * 64 < rbits; ++k) {
+        uint64_t m0 = 64 * k, win = 0;
+        int64_t a = ((int64_t)n - (int64_t)(m0 % n) - 63) % (int64_t)n;
+        if (a < 0) a += n;
+        if ((uint64_t)a + 63 < n) {
+            uint64_t wi = (uint64_t)a >> 6, sh = (uint64_t)a & 63;
+            win = sh ? (S[wi] >> sh) | (S[wi + 1] << (64 - sh)) : S[wi];
+        } else {
+            for (int b = 0; b < 64; ++b) {
+                uint64_t idx = ((uint64_t)a + b) % n;
+                win |= ((S[idx >> 6] >> (idx & 63)) & 1ull) << b;
+            }
+        }
+        c->R[k] = brev64(win);
+    }
+    free(S);
     return c;
 }
 

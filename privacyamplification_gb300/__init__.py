@@ -29,6 +29,7 @@ PA_ERR_TOO_LARGE = -4
 PA_ERR_PRECISION = -5
 FLAG_XOR_KEY_REST = 1
 FLAG_COMPRESS = 2
+FLAG_EXACT = 4
 DEFAULT_FLAGS = FLAG_XOR_KEY_REST | FLAG_COMPRESS
 
 # Every symbol include/pa_gb300.h declares.
@@ -56,7 +57,7 @@ class PAConfig(ctypes.Structure):
 class PAStats(ctypes.Structure):
     _fields_ = [("max_residual", ctypes.c_float), ("popcount_key", ctypes.c_uint64),
                 ("popcount_seed", ctypes.c_uint64), ("gpu_ms", ctypes.c_float),
-                ("seed_uses_left", ctypes.c_int32)]
+                ("seed_uses_left", ctypes.c_int32), ("exact", ctypes.c_int32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -33,6 +33,11 @@ struct pa_engine {
     float2* d_work2 = nullptr;  // pass B output (tile-major)
     float2* d_spec = nullptr;
     int* d_err = nullptr;       // device error word of the bounded TMA waits
+    uint32_t* d_exact_seed = nullptr;  // NTT of the placed seed (exact path), Np words
+    pa::NttTables* ntt = nullptr;      // exact-path twiddle tables
+    bool exact_valid = false;          // d_exact_seed matches the current seed for exact_geom
+    bool last_exact = false;           // the last block ran on the exact path
+    BlockGeom exact_geom{};
     pa::PassMaps maps{};        // tensor maps for the geometry maps_log_n
     int maps_log_n = -1;
     uint32_t* d_planes = nullptr;
@@ -92,13 +97,17 @@ int make_geom(uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
         g->seed_direct = (uint32_t)std::min<uint64_t>(np - g->h, n);
     }
     g->log_n = g->log_np - 1;
+    g->exact_only = 0;
     if (g->log_n <= 14) {
         g->log_n1 = g->log_n2 = 0;
-    } else {
+    } else if (g->log_n <= 26) {
         g->log_n2 = std::min(14, g->log_n - 5);  // rows 2^10..2^14, columns 2^5..2^12
         g->log_n1 = g->log_n - g->log_n2;
+    } else {  // beyond the FP32 path: exact NTT only
+        g->log_n1 = g->log_n2 = 0;
+        g->exact_only = 1;
+        if (g->log_np > 30) return PA_ERR_TOO_LARGE;
     }
-    if (g->log_n1 > 12) return PA_ERR_TOO_LARGE;
     return PA_OK;
 }
 
@@ -118,7 +127,16 @@ int ensure_maps(pa_engine* e, const BlockGeom& g) {
 
 pa::Scratch scratch(pa_engine* e) { return {e->d_work, e->d_work2, e->d_planes, e->d_err, &e->maps}; }
 
+int build_exact_seed(pa_engine* e, const BlockGeom& g, cudaStream_t s) {
+    int rc = pa::launch_exact_seed(g, e->d_seed, e->d_exact_seed, reinterpret_cast<uint32_t*>(e->d_work2), &e->ntt, s);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    e->exact_geom = g;
+    e->exact_valid = true;
+    return PA_OK;
+}
+
 int build_spectrum(pa_engine* e, const BlockGeom& g, cudaStream_t s) {
+    if (g.exact_only) return build_exact_seed(e, g, s);
     int rc = ensure_maps(e, g);
     if (rc) return rc;
     rc = pa::launch_seed_spectrum(g, e->d_seed, e->d_spec, scratch(e), e->d_cnt + 1, e->num_sms, s);
@@ -133,6 +151,7 @@ int seed_common(pa_engine* e, uint32_t n, int32_t reuse, cudaStream_t s) {
     e->seed_n = n;
     e->seed_left = reuse < 0 ? -1 : std::max<int64_t>(reuse, 1);
     e->spec_valid = false;
+    e->exact_valid = false;
     if (is_pow2(n)) {  // placement does not depend on v: build the spectrum now
         BlockGeom g;
         int rc = make_geom(n, n / 2u, PA_FLAG_COMPRESS, &g);
@@ -142,10 +161,35 @@ int seed_common(pa_engine* e, uint32_t n, int32_t reuse, cudaStream_t s) {
     return PA_OK;
 }
 
+// Exact path for one block (the seed's NTT is built on first use and cached with the seed).
+int exact_block(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const BlockGeom& g, uint32_t flags,
+                uint32_t* d_out, cudaStream_t s) {
+    if (!e->exact_valid || !same_seed_geom(e->exact_geom, g)) {
+        int rc = build_exact_seed(e, g, s);
+        if (rc) return rc;
+    }
+    int rc = pa::launch_exact_block(g, d_ks, d_kr, flags, e->d_exact_seed, reinterpret_cast<uint32_t*>(e->d_work),
+                                    reinterpret_cast<uint32_t*>(e->d_work2), d_out, &e->ntt, s);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    // the exact path leaves no residual: report 0 and the reference popcounts are not needed
+    PA_CUDA(e, cudaMemsetAsync(e->d_resid, 0, sizeof(unsigned int), s));
+    return PA_OK;
+}
+
 int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const BlockGeom& g, uint32_t flags,
                  uint32_t* d_out, cudaStream_t s) {
     if (!e->seed_valid || e->seed_left == 0) return PA_ERR_NO_SEED;
     if (g.n != e->seed_n) return PA_ERR_INVALID_ARG;
+    if (g.exact_only || (flags & PA_FLAG_EXACT)) {
+        PA_CUDA(e, cudaEventRecord(e->ev0, s));
+        int rc = exact_block(e, d_ks, d_kr, g, flags, d_out, s);
+        if (rc) return rc;
+        PA_CUDA(e, cudaEventRecord(e->ev1, s));
+        e->last_exact = true;
+        if (e->seed_left > 0) --e->seed_left;
+        return PA_OK;
+    }
+    e->last_exact = false;
     if (!e->spec_valid || !same_seed_geom(e->spec_geom, g)) {
         int rc = build_spectrum(e, g, s);
         if (rc) return rc;
@@ -192,6 +236,7 @@ int read_stats(pa_engine* e, pa_stats* st, float* resid_out) {
         cudaEventElapsedTime(&ms, e->ev0, e->ev1);
         st->gpu_ms = ms;
         st->seed_uses_left = e->seed_left < 0 ? -1 : (int32_t)e->seed_left;
+        st->exact = e->last_exact ? 1 : 0;
     }
     return PA_OK;
 }
@@ -207,6 +252,7 @@ size_t pa_output_bytes(uint32_t n, uint32_t v, uint32_t flags) {
 int pa_kernels_per_block(uint32_t n, uint32_t v, uint32_t flags) {
     BlockGeom g;
     if (make_geom(n, v, flags, &g)) return 0;
+    if (g.exact_only || (flags & PA_FLAG_EXACT)) return pa::exact_kernel_count(g);
     return pa::kernel_count_key_block(g);
 }
 
@@ -233,7 +279,7 @@ int pa_create(const pa_config* cfg, pa_engine** out) {
     e->max_n = cfg->max_sample_size;
     e->residual_limit = cfg->residual_limit > 0.f ? cfg->residual_limit : 0.25f;
     e->cap_log_np = ceil_log2(cfg->max_sample_size);
-    if (e->cap_log_np > 27) {
+    if (e->cap_log_np > 30) {
         delete e;
         return PA_ERR_TOO_LARGE;
     }
@@ -256,11 +302,13 @@ int pa_create(const pa_config* cfg, pa_engine** out) {
     if ((err = cudaMalloc(&e->d_seed, words * 4)) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_out, words * 4)) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_work, (np / 2) * sizeof(float2))) != cudaSuccess) return fail(err);
-    if ((err = cudaMalloc(&e->d_spec, (np / 2) * sizeof(float2))) != cudaSuccess) return fail(err);
+    const size_t np_fp32 = std::min<size_t>(np, size_t(1) << 27);  // the FP32 path stops at n = 2^27
+    if ((err = cudaMalloc(&e->d_spec, (np_fp32 / 2) * sizeof(float2))) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_exact_seed, np * sizeof(uint32_t))) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_work2, (np / 2) * sizeof(float2))) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_err, sizeof(int))) != cudaSuccess) return fail(err);
     cudaMemset(e->d_err, 0, sizeof(int));
-    if ((err = cudaMalloc(&e->d_planes, np / 8 + 256)) != cudaSuccess) return fail(err);
+    if ((err = cudaMalloc(&e->d_planes, np_fp32 / 8 + 256)) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_cnt, 2 * sizeof(unsigned long long))) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_resid, sizeof(unsigned int))) != cudaSuccess) return fail(err);
     cudaMemset(e->d_cnt, 0, 2 * sizeof(unsigned long long));
@@ -279,6 +327,8 @@ void pa_destroy(pa_engine* e) {
     cudaFree(e->d_out);
     cudaFree(e->d_work);
     cudaFree(e->d_spec);
+    cudaFree(e->d_exact_seed);
+    pa::free_ntt_tables(e->ntt);
     cudaFree(e->d_work2);
     cudaFree(e->d_err);
     cudaFree(e->d_planes);
@@ -346,15 +396,22 @@ int pa_process(pa_engine* e, const uint32_t* key_start, const uint32_t* key_rest
     rc = block_common(e, e->d_key_start, e->d_key_rest, g, flags, e->d_out, s);
     if (rc) return rc;
     size_t ob = pa_output_bytes(n, v, flags);
-    PA_CUDA(e, cudaMemcpyAsync(out, e->d_out, ob, cudaMemcpyDeviceToHost, s));
     PA_CUDA(e, cudaStreamSynchronize(s));
     float resid = 0.f;
     rc = read_stats(e, stats, &resid);
     if (rc) return rc;
     if (!(resid <= e->residual_limit)) {
-        std::memset(out, 0, ob);
-        return PA_ERR_PRECISION;
+        // FP32 rounding budget exceeded: recompute this block exactly (same inputs, same seed use)
+        if (e->seed_left >= 0) ++e->seed_left;
+        rc = block_common(e, e->d_key_start, e->d_key_rest, g, flags | PA_FLAG_EXACT, e->d_out, s);
+        if (rc) return rc;
+        PA_CUDA(e, cudaStreamSynchronize(s));
+        float r2 = 0.f;
+        rc = read_stats(e, stats, &r2);
+        if (rc) return rc;
+        if (stats) stats->max_residual = resid;  // report what the FP32 path measured
     }
+    PA_CUDA(e, cudaMemcpy(out, e->d_out, ob, cudaMemcpyDeviceToHost));
     return PA_OK;
 }
 

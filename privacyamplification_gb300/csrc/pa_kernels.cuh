@@ -14,7 +14,8 @@ struct BlockGeom {
     int log_np;            // cyclic length Np = 2^log_np >= n (== n when n is a power of two)
     int log_n;             // complex length N = Np/2
     int log_n1, log_n2;    // three-pass split N = N1 * N2 (0, 0 for the single-CTA path)
-    uint32_t seed_direct;  // seed positions < seed_direct map to themselves (see seed_bit)
+    uint32_t seed_direct;  // seed positions < seed_direct map to themselves (see seed_source)
+    int exact_only;        // 1: beyond the FP32 path (n > 2^27), only the exact NTT path applies
 };
 
 // Seed placement in the cyclic length Np.  For Np == n this is the identity.  For a padded Np the
@@ -70,4 +71,14 @@ int launch_pass_c(const BlockGeom& g, const PassMaps& maps, const float2* Z, con
                   uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s);
 int launch_finish(const BlockGeom& g, const uint32_t* planes, const uint32_t* key_rest, uint32_t flags,
                   uint32_t* out, cudaStream_t s);
+
+// Exact path (pa_ntt.cu): integer convolution modulo 3*2^30+1.  seed_hat, a, tmp: Np words each.
+struct NttTables;
+void free_ntt_tables(NttTables* t);
+int launch_exact_seed(const BlockGeom& g, const uint32_t* seed, uint32_t* seed_hat, uint32_t* tmp,
+                      NttTables** tables, cudaStream_t s);
+int launch_exact_block(const BlockGeom& g, const uint32_t* key_start, const uint32_t* key_rest, uint32_t flags,
+                       const uint32_t* seed_hat, uint32_t* a, uint32_t* tmp, uint32_t* out_words, NttTables** tables,
+                       cudaStream_t s);
+int exact_kernel_count(const BlockGeom& g);
 }  // namespace pa

@@ -1,0 +1,117 @@
+"""Exact integer path (NTT mod 3*2^30+1) and the FP32 precision guard, through the C ABI.
+
+Precision-stress configuration: blocks whose FP32 rounding budget is exceeded (a seed with a long run of
+ones and an all-ones key) must still be bit-exact -- pa_process detects them by their residual and
+recomputes them exactly; n = 2^29 blocks (dynamic seed) run on the exact path only.
+"""
+import numpy as np
+import pytest
+
+import privacyamplification_gb300 as pa
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DEFAULT = pa.FLAG_XOR_KEY_REST | pa.FLAG_COMPRESS
+
+
+def std_sizes(n):
+    return n, n // 4 + n // 8
+
+
+@pytest.mark.parametrize("n,v,flags", [
+    (1 << 10, 384, DEFAULT), (1 << 14, 6144, 0), (1 << 16, 24576, DEFAULT), (1 << 18, 98304, pa.FLAG_COMPRESS),
+    (1 << 20, 393216, DEFAULT), (40960, 15360, DEFAULT), (99328, 9984, 0)])
+def test_exact_flag_matches_oracle(gpu_engine, n, v, flags):
+    seed, recv = O.random_block(n, v, 31 * n + v)
+    ks, kr = O.key_split(recv, n, v)
+    gpu_engine.set_seed(seed, n, -1)
+    out = gpu_engine.process(ks, kr, n, v, flags | pa.FLAG_EXACT)
+    assert gpu_engine.last_stats.exact == 1
+    ref = O.direct(seed, ks, kr, n, v, flags) if n <= 1 << 17 else O.ntt(seed, ks, kr, n, v, flags)
+    assert np.array_equal(out, ref)
+    assert np.array_equal(gpu_engine.process(ks, kr, n, v, flags), ref)  # FP32 path agrees
+    assert gpu_engine.last_stats.exact == 0
+
+
+def run_structured(n, v):
+    """Seed: first n/2 bits one; key: all ones -- the FP32-breaking block."""
+    seed = np.zeros(n // 32, np.uint32)
+    seed[: n // 64] = 0xFFFFFFFF
+    recv = np.full(n // 32 + 1, 0xFFFFFFFF, np.uint32)
+    return seed, recv
+
+
+@pytest.mark.parametrize("logn", [22, 24])
+def test_guard_falls_back_to_exact(gpu_engine, logn):
+    n, v = std_sizes(1 << logn)
+    seed, recv = run_structured(n, v)
+    ks, kr = O.key_split(recv, n, v)
+    gpu_engine.set_seed(seed, n, -1)
+    out = gpu_engine.process(ks, kr, n, v)
+    st = gpu_engine.last_stats
+    assert st.max_residual > 0.25, "the FP32 path was expected to exceed its budget on this block"
+    assert st.exact == 1
+    assert np.array_equal(out, O.ntt(seed, ks, kr, n, v))
+
+
+def test_all_ones_block_is_benign(gpu_engine):
+    """All-ones key and seed: the seed spectrum is pure DC, which the path drops, so FP32 stays exact."""
+    n, v = std_sizes(1 << 22)
+    seed = np.full(n // 32, 0xFFFFFFFF, np.uint32)
+    recv = np.full(n // 32 + 1, 0xFFFFFFFF, np.uint32)
+    ks, kr = O.key_split(recv, n, v)
+    gpu_engine.set_seed(seed, n, -1)
+    out = gpu_engine.process(ks, kr, n, v)
+    assert gpu_engine.last_stats.exact == 0
+    assert np.array_equal(out, O.ntt(seed, ks, kr, n, v))
+
+
+def test_adversarial_2p27_sampled_rows(gpu_engine):
+    n, v = 1 << 27, 50331648
+    seed, recv = run_structured(n, v)
+    ks, kr = O.key_split(recv, n, v)
+    gpu_engine.set_seed(seed, n, -1)
+    out = gpu_engine.process(ks, kr, n, v)
+    assert gpu_engine.last_stats.exact == 1
+    blk = O.DirectBlock(seed, ks, n, v)
+    krb = O.bits_msb(kr, v).astype(np.uint8)
+    for r0 in (0, 64 * 12345, v // 2, v - 64):
+        ref = blk.rows(r0, r0 + 64) ^ krb[r0: r0 + 64]
+        assert np.array_equal(np.unpackbits(out[r0 // 8: r0 // 8 + 8]), ref), r0
+
+
+@pytest.fixture(scope="module")
+def big_engine(pa_lib):
+    eng = pa.Engine(max_sample_size=1 << 29)
+    yield eng
+    eng.close()
+
+
+def test_config3_2p29_dynamic_seed(big_engine):
+    """n = 2^29, h = n/2+n/8, v = n/4+n/8, a fresh seed per block: sampled rows against the direct
+    oracle, GF(2) linearity in the key for a fixed seed, and the key_rest XOR."""
+    n, v = std_sizes(1 << 29)
+    rng = np.random.default_rng(29)
+    outs = []
+    for blk_no in range(2):
+        seed, recv = O.random_block(n, v, 2900 + blk_no)
+        ks, kr = O.key_split(recv, n, v)
+        big_engine.set_seed(seed, n, 0)
+        out = big_engine.process(ks, kr, n, v)
+        assert big_engine.last_stats.exact == 1
+        blk = O.DirectBlock(seed, ks, n, v)
+        krb = O.bits_msb(kr, v).astype(np.uint8)
+        for r0 in [0, v - 64] + [int(x) * 64 for x in rng.integers(0, v // 64, 3)]:
+            ref = blk.rows(r0, r0 + 64) ^ krb[r0: r0 + 64]
+            assert np.array_equal(np.unpackbits(out[r0 // 8: r0 // 8 + 8]), ref), (blk_no, r0)
+        outs.append((seed, ks, kr, out))
+    seed, ks1, kr1, _ = outs[1]
+    _, ks2, _, _ = outs[0]
+    big_engine.set_seed(seed, n, -1)
+    o1 = big_engine.process(ks1, kr1, n, v, pa.FLAG_COMPRESS)
+    o2 = big_engine.process(ks2, kr1, n, v, pa.FLAG_COMPRESS)
+    o12 = big_engine.process(ks1 ^ ks2, kr1, n, v, pa.FLAG_COMPRESS)
+    assert np.array_equal(o12, o1 ^ o2)
+    ox = big_engine.process(ks1, kr1, n, v, DEFAULT)
+    assert np.array_equal(ox, o1 ^ kr1.astype(">u4").view(np.uint8))
