@@ -121,6 +121,20 @@ PA_API int pa_stage_times(pa_engine* e, float* ms, int max_stages, int* nstages,
 PA_API const char* pa_error_string(int code);
 PA_API int pa_last_cuda_error(pa_engine* e);
 
+/* No counterpart in the reference.  One block hashed with its own seed, without any engine and without
+ * allocating device memory: for callers that may not call cudaMalloc (device memory owned by another
+ * allocator, or a memory map fixed at start-up).  All pointers are device memory the caller owns:
+ * d_seed_words n/32 words, d_key_start and d_key_rest as for pa_process_device (d_key_rest may be NULL
+ * when PA_FLAG_XOR_KEY_REST is clear), d_out (4-byte aligned) pa_output_bytes() bytes rounded up to a
+ * multiple of 4.  Work is queued on `stream` (a cudaStream_t; NULL = the legacy default stream) and the
+ * call returns without synchronising; no statistics are produced and the precision guard does not run.
+ * Limit: n <= 32768 (padded cyclic length <= 32768); larger n returns PA_ERR_TOO_LARGE, and
+ * PA_FLAG_EXACT returns PA_ERR_INVALID_ARG.  The scratch (132 KiB) is a static device array of the
+ * library, one per GPU: the first call on a device looks up its address (make it before any stream
+ * capture), and calls that overlap on one GPU race on it. */
+PA_API int pa_process_noalloc(const uint32_t* d_seed_words, const uint32_t* d_key_start, const uint32_t* d_key_rest,
+                              uint32_t n, uint32_t v, uint32_t flags, uint8_t* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,7 +35,7 @@ DEFAULT_FLAGS = FLAG_XOR_KEY_REST | FLAG_COMPRESS
 # Every symbol include/pa_gb300.h declares.
 EXPORTS = ("pa_create", "pa_destroy", "pa_set_seed", "pa_process", "pa_set_seed_device", "pa_process_device",
            "pa_sync", "pa_key_split", "pa_output_bytes", "pa_kernels_per_block", "pa_set_timing",
-           "pa_stage_times", "pa_error_string", "pa_last_cuda_error")
+           "pa_stage_times", "pa_error_string", "pa_last_cuda_error", "pa_process_noalloc")
 
 
 class PAError(RuntimeError):
@@ -94,6 +94,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                             ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "pa_error_string": ([ctypes.c_int], ctypes.c_char_p),
         "pa_last_cuda_error": ([eng], ctypes.c_int),
+        "pa_process_noalloc": ([vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -113,6 +114,16 @@ def output_bytes(n: int, v: int, flags: int = DEFAULT_FLAGS) -> int:
 
 def kernels_per_block(n: int, v: int, flags: int = DEFAULT_FLAGS) -> int:
     return int(load_library().pa_kernels_per_block(n, v, flags))
+
+
+def process_noalloc(d_seed: int, d_key_start: int, d_key_rest: int, n: int, v: int, d_out: int,
+                    flags: int = DEFAULT_FLAGS, stream: int = 0):
+    """pa_process_noalloc: one block (n <= 2^15) with its own seed, device pointers only, no engine and no
+    device allocation; queued on `stream`, returns without synchronising."""
+    rc = load_library().pa_process_noalloc(d_seed, d_key_start, d_key_rest or None, n, v, flags, d_out,
+                                           stream or None)
+    if rc != 0:
+        raise PAError(rc, "pa_process_noalloc")
 
 
 def _u32(a) -> np.ndarray:
