@@ -15,6 +15,10 @@ reference's definition (PrivacyAmplification.cu:1213, 2081).
 * roofline -- the dominant kernel's algorithmic bytes per launch / its mean CUDA-event duration in
             the timed region, against MEASURED_PEAKS.json's hbm_gbs.
 * cpu_baseline -- the exact NTT convolution of the oracle on all host cores, one whole block.
+* cufft_plain -- the reference's plain single-block GPU pipeline restated on cuFFT
+            (baseline/cufft_plain.cu: its kernels, launch shapes, pinned zero-copy slots and host syncs)
+            on the same GPU and inputs, static and dynamic seed, host wall time per block as the
+            reference's speedtest measures it; plus whether its output bytes equal the engine's.
 * --impl reference -- the reference has no CPU implementation of the path and its CUDA build cannot
             run here (its sources are not on the GPU host), so this arm times the CPU port of the
             GF(2) Toeplitz product (oracle, direct bit-packed rows) with all host threads on the same
@@ -170,6 +174,45 @@ def cpu_baseline(threads=0):
     return N_BITS / dt / 1e9, cores, sample
 
 
+def cufft_plain_leg(seed, keys, eng, steps):
+    """Times the cuFFT pipeline baseline (4 warm-up blocks, then `steps` blocks per seed mode) and
+    checks its output bytes against the engine's on the same key."""
+    import numpy as np
+    from baseline import cufft_plain
+    cufft_plain.build()
+    cp = cufft_plain.CufftPlain(N_BITS, V_BITS)
+    try:
+        cp.load(seed=seed)
+        res = {}
+        for mode, recalc in (("static", False), ("dynamic", True)):
+            times = []
+            for i in range(4 + steps):
+                ks, kr = keys[i % len(keys)]
+                cp.load(key_start=ks, key_rest=kr)  # outside the timed call, like a filled ring slot
+                ms = cp.process(recalc_seed=recalc or i == 0)
+                if i >= 4:
+                    times.append(ms)
+            times.sort()
+            p50 = times[len(times) // 2]
+            p99 = times[min(len(times) - 1, int(round(0.99 * (len(times) - 1))))]
+            res[mode] = {"value": N_BITS / (p50 / 1e3) / 1e9, "unit": UNIT, "p50_ms": p50, "p99_ms": p99,
+                         "blocks": len(times)}
+        ks, kr = keys[0]
+        cp.load(key_start=ks, key_rest=kr)
+        cp.process(recalc_seed=False)
+        nbytes = V_BITS // 8
+        theirs = cp.output(nbytes)
+        resid = cp.residual(V_BITS)
+        mine = eng.process(ks, kr, N_BITS, V_BITS)
+        res["output_equal"] = bool(np.array_equal(theirs, mine))
+        res["max_residual"] = resid
+        res["what"] = ("reference mainloop sequence restated on cuFFT (baseline/cufft_plain.cu): zero-copy "
+                       "pinned slots, per-step host syncs; wall ms per block, value at p50")
+        return res
+    finally:
+        cp.close()
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -322,6 +365,8 @@ def run_ours(args):
     block_bytes = 20 * n + ((H_BITS + 1) + 2 * V_BITS) // 8
     total_s = sum(stage_ms) / 1e3 if stage_ms else None
 
+    plain = None if args.no_cufft else cufft_plain_leg(seed, keys, eng, min(args.steps, 20))
+
     if args.no_cpu:
         cpu = None
     else:
@@ -344,6 +389,7 @@ def run_ours(args):
                             if total_s else None},
         "roofline": roof,
         "cpu_baseline": cpu,
+        "cufft_plain": plain,
         "clocks": clk.summary(),
         "max_residual": stats.max_residual,
     }
@@ -361,6 +407,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT pipeline baseline leg")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -63,3 +63,13 @@ def test_key_split_rejects_bad_sizes(pa_lib):
 def test_error_strings(pa_lib):
     assert pa.error_string(pa.PA_OK) == "ok"
     assert "seed" in pa.error_string(pa.PA_ERR_NO_SEED)
+
+
+def test_cufft_baseline_builds_and_exports():
+    """The cuFFT pipeline baseline (timed beside the engine) builds for sm_103a and exports its entry points."""
+    import ctypes
+    from baseline import cufft_plain
+    lib = ctypes.CDLL(cufft_plain.build())
+    for name in ("cp_create", "cp_destroy", "cp_seed_slot", "cp_key_start_slot", "cp_key_rest_slot",
+                 "cp_output_slot", "cp_process", "cp_residual"):
+        assert hasattr(lib, name), name

@@ -1,0 +1,77 @@
+"""The engine against the reference's plain cuFFT pipeline (baseline/cufft_plain.cu) on the same inputs.
+
+Both must equal the oracle where the oracle finishes quickly; at n = 2^27 the engine's output must be
+SHA3-equal to the cuFFT pipeline's on identical inputs (the reference's own 2^27 golden files are not
+available, so this is the stand-in for its SHA3 check).
+"""
+import numpy as np
+import pytest
+
+import privacyamplification_gb300 as pa
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DEFAULT = pa.FLAG_XOR_KEY_REST | pa.FLAG_COMPRESS
+
+
+@pytest.fixture(scope="module")
+def plain_lib():
+    from baseline import cufft_plain
+    cufft_plain.build()
+    return cufft_plain
+
+
+def flags_of(do_xor, do_compress):
+    return (pa.FLAG_XOR_KEY_REST if do_xor else 0) | (pa.FLAG_COMPRESS if do_compress else 0)
+
+
+@pytest.mark.parametrize("logn,do_xor,do_compress", [(16, True, True), (16, False, False), (18, False, True),
+                                                      (20, True, True)])
+def test_plain_matches_oracle_and_engine(plain_lib, gpu_engine, logn, do_xor, do_compress):
+    n = 1 << logn
+    v = n // 4 + n // 8
+    flags = flags_of(do_xor, do_compress)
+    cp = plain_lib.CufftPlain(n, v)
+    seed, _ = O.random_block(n, v, 500 + logn)
+    try:
+        for blk in range(3):  # static seed: computed on the first block, reused after
+            _, recv = O.random_block(n, v, 900 + 7 * logn + blk)
+            ks, kr = O.key_split(recv, n, v)
+            cp.load(seed=seed if blk == 0 else None, key_start=ks, key_rest=kr)
+            cp.process(recalc_seed=(blk == 0), do_xor=do_xor, do_compress=do_compress)
+            ob = pa.output_bytes(n, v, flags)
+            got = cp.output(ob)
+            gpu_engine.set_seed(seed, n, -1)
+            mine = gpu_engine.process(ks, kr, n, v, flags)
+            assert np.array_equal(got, mine), blk
+            if n <= 1 << 16:
+                assert np.array_equal(got, O.direct(seed, ks, kr, n, v, flags)), blk
+            else:
+                assert np.array_equal(got, O.ntt(seed, ks, kr, n, v, flags)), blk
+    finally:
+        cp.close()
+
+
+def test_2p27_sha3_equal_to_plain_cufft(plain_lib, gpu_engine):
+    """Config-2 size: engine bits SHA3-equal to the cuFFT pipeline's on the same inputs, static seed,
+    two consecutive key blocks, plus both residuals well inside the rounding budget."""
+    n, v = 1 << 27, 50331648
+    seed, recv = O.random_block(n, v, 0x5EED)
+    cp = plain_lib.CufftPlain(n, v)
+    try:
+        gpu_engine.set_seed(seed, n, -1)
+        cp.load(seed=seed)
+        for blk in range(2):
+            if blk:
+                _, recv = O.random_block(n, v, 0x5EED + blk)
+            ks, kr = O.key_split(recv, n, v)
+            cp.load(key_start=ks, key_rest=kr)
+            cp.process(recalc_seed=(blk == 0))
+            got = cp.output(v // 8)
+            mine = gpu_engine.process(ks, kr, n, v, DEFAULT)
+            assert O.sha3_256(got.tobytes()) == O.sha3_256(mine.tobytes()), blk
+            assert cp.residual(v) < 0.25
+            assert gpu_engine.last_stats.max_residual < 0.25
+    finally:
+        cp.close()
