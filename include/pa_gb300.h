@@ -121,6 +121,65 @@ PA_API int pa_stage_times(pa_engine* e, float* ms, int max_stages, int* nstages,
 PA_API const char* pa_error_string(int code);
 PA_API int pa_last_cuda_error(pa_engine* e);
 
+/* ---- Batched and served blocks -------------------------------------------------------------------
+ * No counterpart in the reference: its mainloop (PrivacyAmplification.cu:1686-2118) runs one block at
+ * a time with a host sync after every step.  Here blocks of different sizes run concurrently on a pool
+ * of slots; a slot is a CUDA stream with its own working set (about 12.6 * Np bytes for cyclic length
+ * Np), created on demand within the pool's HBM budget.  Sizes: the FP32 path (n <= 2^27); a block
+ * whose residual exceeds residual_limit is recomputed on the exact path when its result is collected
+ * (pa_batch_sync, pa_poll), as in pa_process. */
+#define PA_ERR_BUSY (-6) /* pa_submit: no slot or HBM free now; collect a block with pa_poll and retry */
+#define PA_PENDING 1     /* pa_poll: the block is still running */
+
+typedef struct pa_job {
+    const uint32_t* seed_words; /* n/32 words: the block's own (dynamic) seed; NULL when seed_id >= 0 */
+    int32_t seed_id;            /* static seed: a spectrum from pa_seed_cache_add, or -1 */
+    const uint32_t* key_start;  /* n/32 words as from pa_key_split (words past h/32 are not read) */
+    const uint32_t* key_rest;   /* v/32 words; may be NULL when PA_FLAG_XOR_KEY_REST is clear */
+    uint32_t n, v, flags;       /* PA_FLAG_EXACT is not accepted here */
+    uint8_t* out;               /* pa_output_bytes() bytes (device pointers: 4-byte aligned, rounded up to 4) */
+} pa_job;
+
+/* Pool limits: HBM bytes all slots may hold (0 = 60 % of the free memory at first use), the number
+ * of slots (0 = 16) and the slots one batch spreads over (0 = 8).  Idle slots are freed first. */
+PA_API int pa_set_pool(pa_engine* e, uint64_t hbm_budget_bytes, int32_t max_slots, int32_t batch_slots);
+
+/* Static seeds: computes and keeps the FP32 spectrum of a seed (host words, n/32) for blocks of
+ * geometry (n, v, flags) -- for a power-of-two n any v and flags share it.  Synchronous.  The id is
+ * valid until pa_seed_cache_clear.  Replaces the reference's reuse of do2 across blocks
+ * (PrivacyAmplification.cu:1903, reuse_seed_amount) for many seeds at once. */
+PA_API int pa_seed_cache_add(pa_engine* e, const uint32_t* seed_words, uint32_t n, uint32_t v, uint32_t flags,
+                             int32_t* seed_id);
+PA_API int pa_seed_cache_clear(pa_engine* e);
+
+/* Batch of blocks with DEVICE pointers, queued on `stream` (NULL = the engine's stream); returns
+ * without synchronising.  Jobs are spread over the pool's batch slots, longest first.
+ * PA_BATCH_GRAPH: capture the whole batch as one CUDA graph the first time these exact jobs are seen
+ * and replay it afterwards.  PA_BATCH_SERIAL: one slot, jobs in order (the per-block launch
+ * sequence, for comparison).  pa_batch_sync waits, recomputes blocks over the residual limit
+ * exactly, and fills stats[i] for job i (gpu_ms: the whole batch's device time). */
+#define PA_BATCH_GRAPH 1u
+#define PA_BATCH_SERIAL 2u
+PA_API int pa_batch_run(pa_engine* e, const pa_job* jobs, uint32_t count, uint32_t batch_flags, void* stream);
+PA_API int pa_batch_sync(pa_engine* e, pa_stats* stats, uint32_t count);
+
+/* Served blocks with HOST pointers (pinned memory lets the copies overlap): pa_submit admits the
+ * block to a free slot (creating one if the HBM budget allows), queues copy-in, kernels and copy-out,
+ * and returns a ticket; PA_ERR_BUSY when nothing is free.  pa_poll returns PA_PENDING while the block
+ * runs, then PA_OK once job->out holds the result (stats filled, slot released).  The job's host
+ * buffers must stay valid until then. */
+PA_API int pa_submit(pa_engine* e, const pa_job* job, uint64_t* ticket);
+PA_API int pa_poll(pa_engine* e, uint64_t ticket, pa_stats* stats);
+
+/* Three-pass split (N = N1 * N2, N = Np/2): pa_set_split fixes log2 N2 for log2 N = log_n (row FFT
+ * length; allowed max(10, log_n-12) .. min(14, log_n-5)); pa_get_split returns the one in use.
+ * pa_autotune times every allowed split of each log_n in [log2(min_n)-1, log2(max_n)-1] on a synthetic
+ * block and keeps the fastest; ms_out (optional, 32 floats) receives the best key-block time per
+ * log_n.  Cached spectra keep the split they were built with. */
+PA_API int pa_set_split(pa_engine* e, uint32_t log_n, uint32_t log_n2);
+PA_API int pa_get_split(pa_engine* e, uint32_t log_n);
+PA_API int pa_autotune(pa_engine* e, uint32_t min_n, uint32_t max_n, float* ms_out);
+
 /* No counterpart in the reference.  One block hashed with its own seed, without any engine and without
  * allocating device memory: for callers that may not call cudaMalloc (device memory owned by another
  * allocator, or a memory map fixed at start-up).  All pointers are device memory the caller owns:

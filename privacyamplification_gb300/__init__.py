@@ -27,6 +27,10 @@ PA_ERR_CUDA = -2
 PA_ERR_NO_SEED = -3
 PA_ERR_TOO_LARGE = -4
 PA_ERR_PRECISION = -5
+PA_ERR_BUSY = -6
+PA_PENDING = 1
+BATCH_GRAPH = 1
+BATCH_SERIAL = 2
 FLAG_XOR_KEY_REST = 1
 FLAG_COMPRESS = 2
 FLAG_EXACT = 4
@@ -35,7 +39,9 @@ DEFAULT_FLAGS = FLAG_XOR_KEY_REST | FLAG_COMPRESS
 # Every symbol include/pa_gb300.h declares.
 EXPORTS = ("pa_create", "pa_destroy", "pa_set_seed", "pa_process", "pa_set_seed_device", "pa_process_device",
            "pa_sync", "pa_key_split", "pa_output_bytes", "pa_kernels_per_block", "pa_set_timing",
-           "pa_stage_times", "pa_error_string", "pa_last_cuda_error", "pa_process_noalloc")
+           "pa_stage_times", "pa_error_string", "pa_last_cuda_error", "pa_process_noalloc", "pa_set_pool",
+           "pa_seed_cache_add", "pa_seed_cache_clear", "pa_batch_run", "pa_batch_sync", "pa_submit", "pa_poll",
+           "pa_set_split", "pa_get_split", "pa_autotune")
 
 
 class PAError(RuntimeError):
@@ -61,6 +67,13 @@ class PAStats(ctypes.Structure):
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class PAJob(ctypes.Structure):
+    """pa_job: one block of a batch (device pointers) or a served request (host pointers)."""
+    _fields_ = [("seed_words", ctypes.c_void_p), ("seed_id", ctypes.c_int32), ("key_start", ctypes.c_void_p),
+                ("key_rest", ctypes.c_void_p), ("n", ctypes.c_uint32), ("v", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("out", ctypes.c_void_p)]
 
 
 _lib = None
@@ -95,6 +108,17 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pa_error_string": ([ctypes.c_int], ctypes.c_char_p),
         "pa_last_cuda_error": ([eng], ctypes.c_int),
         "pa_process_noalloc": ([vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp], ctypes.c_int),
+        "pa_set_pool": ([eng, ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+        "pa_seed_cache_add": ([eng, u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                               ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+        "pa_seed_cache_clear": ([eng], ctypes.c_int),
+        "pa_batch_run": ([eng, ctypes.POINTER(PAJob), ctypes.c_uint32, ctypes.c_uint32, vp], ctypes.c_int),
+        "pa_batch_sync": ([eng, ctypes.POINTER(PAStats), ctypes.c_uint32], ctypes.c_int),
+        "pa_submit": ([eng, ctypes.POINTER(PAJob), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+        "pa_poll": ([eng, ctypes.c_uint64, ctypes.POINTER(PAStats)], ctypes.c_int),
+        "pa_set_split": ([eng, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+        "pa_get_split": ([eng, ctypes.c_uint32], ctypes.c_int),
+        "pa_autotune": ([eng, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -229,6 +253,62 @@ class Engine:
         ns, nb = ctypes.c_int(), ctypes.c_int()
         self._check(self._lib.pa_stage_times(self._h, ms, 8, ctypes.byref(ns), ctypes.byref(nb)), "pa_stage_times")
         return [ms[i] for i in range(ns.value)], nb.value
+
+    # ---- batched and served blocks (slot pool) ------------------------------------------------------
+    def set_pool(self, hbm_budget_bytes: int = 0, max_slots: int = 0, batch_slots: int = 0):
+        self._check(self._lib.pa_set_pool(self._h, hbm_budget_bytes, max_slots, batch_slots), "pa_set_pool")
+
+    def seed_cache_add(self, seed_words, n: int, v: int, flags: int = DEFAULT_FLAGS) -> int:
+        s = _u32(seed_words)
+        if s.size < n // 32:
+            raise ValueError("seed needs n/32 words")
+        sid = ctypes.c_int32()
+        self._check(self._lib.pa_seed_cache_add(self._h, _p32(s), n, v, flags, ctypes.byref(sid)),
+                    "pa_seed_cache_add")
+        return sid.value
+
+    def seed_cache_clear(self):
+        self._check(self._lib.pa_seed_cache_clear(self._h), "pa_seed_cache_clear")
+
+    def batch_run(self, jobs, batch_flags: int = 0, stream: int = 0):
+        """jobs: a sequence of PAJob with device pointers (integers)."""
+        arr = (PAJob * max(1, len(jobs)))(*jobs)
+        self._check(self._lib.pa_batch_run(self._h, arr, len(jobs), batch_flags, stream or None), "pa_batch_run")
+
+    def batch_sync(self, count: int):
+        st = (PAStats * max(1, count))()
+        self._check(self._lib.pa_batch_sync(self._h, st, count), "pa_batch_sync")
+        return [st[i] for i in range(count)]
+
+    def submit(self, job: PAJob):
+        """Returns a ticket, or None when no slot / HBM is free now (PA_ERR_BUSY)."""
+        t = ctypes.c_uint64()
+        rc = self._lib.pa_submit(self._h, ctypes.byref(job), ctypes.byref(t))
+        if rc == PA_ERR_BUSY:
+            return None
+        self._check(rc, "pa_submit")
+        return t.value
+
+    def poll(self, ticket: int):
+        """None while the block runs; its PAStats once its output is in the job's host buffer."""
+        st = PAStats()
+        rc = self._lib.pa_poll(self._h, ticket, ctypes.byref(st))
+        if rc == PA_PENDING:
+            return None
+        self._check(rc, "pa_poll")
+        return st
+
+    def set_split(self, log_n: int, log_n2: int):
+        self._check(self._lib.pa_set_split(self._h, log_n, log_n2), "pa_set_split")
+
+    def get_split(self, log_n: int) -> int:
+        return int(self._lib.pa_get_split(self._h, log_n))
+
+    def autotune(self, min_n: int, max_n: int):
+        """Times every split of each size class in [min_n, max_n]; returns {log_n: (log_n2, best ms)}."""
+        ms = (ctypes.c_float * 32)()
+        self._check(self._lib.pa_autotune(self._h, min_n, max_n, ms), "pa_autotune")
+        return {i: (self.get_split(i), ms[i]) for i in range(32) if ms[i] > 0}
 
     def sync(self, check: bool = True) -> PAStats:
         rc = self._lib.pa_sync(self._h, ctypes.byref(self.last_stats))

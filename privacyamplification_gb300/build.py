@@ -16,8 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpa_gb300.so")
-SOURCES = ["pa_kernels.cu", "pa_passes.cu", "pa_ntt.cu", "pa_engine.cu", "pa_noalloc.cu"]
-HEADERS = ["pa_device.cuh", "pa_fft.cuh", "pa_tma.cuh", "pa_kernels.cuh", os.path.join("..", "..", "include", "pa_gb300.h")]
+SOURCES = ["pa_kernels.cu", "pa_passes.cu", "pa_ntt.cu", "pa_engine.cu", "pa_batch.cu", "pa_noalloc.cu"]
+HEADERS = ["pa_device.cuh", "pa_fft.cuh", "pa_tma.cuh", "pa_kernels.cuh", "pa_engine_impl.h", os.path.join("..", "..", "include", "pa_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]

@@ -1,0 +1,797 @@
+// pa_batch.cu -- many blocks on one GPU: a pool of slots (one CUDA stream + working set each), the
+// static-seed spectrum cache, batched runs (optionally one CUDA graph per batch), served blocks
+// (pa_submit / pa_poll, admission by free slot and HBM budget) and the three-pass split autotuner.
+//
+// The reference has none of this (one block at a time, PrivacyAmplification.cu:1686-2118); the
+// per-block work is the same key-block / seed-spectrum kernels the single-block engine runs.
+#include "pa_engine_impl.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <unordered_map>
+#include <vector>
+
+using pa::BlockGeom;
+
+namespace pa_host {
+
+namespace {
+
+constexpr int kFp32MaxLogNp = 27;  // the FP32 path serves n <= 2^27
+
+struct Mirror {  // pinned host copy of a served block's statistics
+    unsigned long long cnt[2];
+    unsigned int resid;
+    int err;
+};
+
+struct SeedEntry {
+    BlockGeom g{};
+    float2* spec = nullptr;          // FP32 spectrum in the key path's layout
+    uint32_t* seed = nullptr;        // seed words (for the exact recompute)
+    unsigned long long* cnt = nullptr;  // popcount of the placed seed
+    size_t bytes = 0;
+    bool live = false;
+};
+
+}  // namespace
+
+struct Slot {
+    int cap = 0;  // log2 of the largest cyclic length the buffers hold
+    size_t bytes = 0;
+    cudaStream_t s = nullptr;
+    float2* work = nullptr;   // pass A output / exact-path residues
+    float2* work2 = nullptr;  // pass B output / exact-path scratch
+    float2* spec = nullptr;   // dynamic seed spectrum / exact seed transform
+    uint32_t* planes = nullptr;
+    int* err = nullptr;
+    unsigned long long* cnt = nullptr;  // served block: [0] key, [1] seed popcount
+    unsigned int* resid = nullptr;
+    uint32_t *seed = nullptr, *ks = nullptr, *kr = nullptr, *out = nullptr;  // served-block staging
+    Mirror* host = nullptr;
+    pa::PassMaps maps{};
+    int maps_key = -1;
+    pa::NttTables* ntt = nullptr;
+    cudaEvent_t done = nullptr, join = nullptr;
+    // served block in flight
+    bool busy = false;
+    uint64_t ticket = 0;
+    pa_job job{};
+    BlockGeom g{};
+    int seed_id = -1;
+    uint64_t last_use = 0;
+};
+
+struct Pool {
+    std::vector<Slot*> slots;
+    std::vector<SeedEntry> seeds;
+    uint64_t budget = 0;
+    size_t used = 0;
+    int max_slots = 16;
+    int batch_slots = 8;
+    uint64_t clock = 0;
+    uint64_t next_ticket = 1;
+    // batch state
+    cudaEvent_t fork = nullptr, b0 = nullptr, b1 = nullptr;
+    unsigned long long* job_cnt = nullptr;  // [count][2]
+    unsigned int* job_resid = nullptr;      // [count]
+    uint32_t job_cap = 0;
+    std::vector<pa_job> jobs;
+    std::vector<BlockGeom> geoms;
+    std::vector<int> job_slot;
+    cudaStream_t batch_stream = nullptr;
+    bool batch_pending = false;
+    std::unordered_map<uint64_t, cudaGraphExec_t> graphs;
+};
+
+namespace {
+
+void free_slot(Pool* p, Slot* sl) {
+    if (!sl) return;
+    if (sl->s) cudaStreamSynchronize(sl->s);
+    cudaFree(sl->work);
+    cudaFree(sl->work2);
+    cudaFree(sl->spec);
+    cudaFree(sl->planes);
+    cudaFree(sl->err);
+    cudaFree(sl->cnt);
+    cudaFree(sl->resid);
+    cudaFree(sl->seed);
+    cudaFree(sl->ks);
+    cudaFree(sl->kr);
+    cudaFree(sl->out);
+    cudaFreeHost(sl->host);
+    pa::free_ntt_tables(sl->ntt);
+    if (sl->done) cudaEventDestroy(sl->done);
+    if (sl->join) cudaEventDestroy(sl->join);
+    if (sl->s) cudaStreamDestroy(sl->s);
+    p->used -= std::min(p->used, sl->bytes);
+    delete sl;
+}
+
+size_t slot_bytes(int cap) {
+    const size_t np = size_t(1) << cap;
+    const size_t np32 = std::min(np, size_t(1) << kFp32MaxLogNp);
+    return 3 * (np / 2) * sizeof(float2) - (np - np32) / 2 * sizeof(float2) + 5 * (np / 8 + 256);
+}
+
+int new_slot(pa_engine* e, Pool* p, int cap, Slot** out) {
+    Slot* sl = new (std::nothrow) Slot();
+    if (!sl) return PA_ERR_INVALID_ARG;
+    sl->cap = cap;
+    const size_t np = size_t(1) << cap;
+    const size_t np32 = std::min(np, size_t(1) << kFp32MaxLogNp);
+    const size_t words = np / 32 + 64;
+    cudaError_t err = cudaSuccess;
+    auto A = [&](void** ptr, size_t bytes) {
+        if (err == cudaSuccess) err = cudaMalloc(ptr, bytes);
+    };
+    A((void**)&sl->work, (np / 2) * sizeof(float2));
+    A((void**)&sl->work2, (np / 2) * sizeof(float2));
+    A((void**)&sl->spec, (np32 / 2) * sizeof(float2));
+    A((void**)&sl->planes, np32 / 8 + 256);
+    A((void**)&sl->err, sizeof(int));
+    A((void**)&sl->cnt, 2 * sizeof(unsigned long long));
+    A((void**)&sl->resid, sizeof(unsigned int));
+    A((void**)&sl->seed, words * 4);
+    A((void**)&sl->ks, words * 4);
+    A((void**)&sl->kr, words * 4);
+    A((void**)&sl->out, words * 4);
+    if (err == cudaSuccess) err = cudaMallocHost((void**)&sl->host, sizeof(Mirror));
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&sl->s, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&sl->join, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaMemset(sl->err, 0, sizeof(int));
+    sl->bytes = slot_bytes(cap);
+    p->used += sl->bytes;
+    if (err != cudaSuccess) {
+        free_slot(p, sl);
+        return cuda_fail(e, err);
+    }
+    *out = sl;
+    return PA_OK;
+}
+
+Pool* get_pool(pa_engine* e) {
+    if (e->pool) return e->pool;
+    Pool* p = new (std::nothrow) Pool();
+    if (!p) return nullptr;
+    if (cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&p->b0) != cudaSuccess || cudaEventCreate(&p->b1) != cudaSuccess) {
+        delete p;
+        return nullptr;
+    }
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    p->budget = (uint64_t)(0.6 * (double)fr);
+    e->pool = p;
+    return p;
+}
+
+void drop_graphs(Pool* p) {
+    for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second);
+    p->graphs.clear();
+}
+
+int ensure_slot_maps(pa_engine* e, Slot* sl, const BlockGeom& g) {
+    if (g.log_n1 == 0 || sl->maps_key == maps_key(g)) return PA_OK;
+    int rc = pa::make_pass_maps(g, sl->work, sl->work2, &sl->maps);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    sl->maps_key = maps_key(g);
+    return PA_OK;
+}
+
+pa::Scratch slot_scratch(Slot* sl) { return {sl->work, sl->work2, sl->planes, sl->err, &sl->maps}; }
+
+int seed_in_slot(pa_engine* e, Slot* sl, const BlockGeom& g, const uint32_t* d_seed, float2* spec,
+                 unsigned long long* cnt_seed, cudaStream_t s) {
+    int rc = ensure_slot_maps(e, sl, g);
+    if (rc) return rc;
+    rc = pa::launch_seed_spectrum(g, d_seed, spec, slot_scratch(sl), cnt_seed, e->num_sms, s);
+    return rc ? cuda_fail(e, (cudaError_t)rc) : PA_OK;
+}
+
+int key_in_slot(pa_engine* e, Slot* sl, const BlockGeom& g, const uint32_t* ks, const uint32_t* kr, uint32_t flags,
+                const float2* spec, unsigned long long* cnt, unsigned int* resid, uint32_t* out, cudaStream_t s) {
+    int rc = ensure_slot_maps(e, sl, g);
+    if (rc) return rc;
+    rc = pa::launch_key_block(g, ks, kr, flags, spec, slot_scratch(sl), cnt, resid, out, e->num_sms, s, nullptr);
+    return rc ? cuda_fail(e, (cudaError_t)rc) : PA_OK;
+}
+
+// Exact recompute of one block in a slot (its spectrum buffer holds the seed transform).
+int exact_in_slot(pa_engine* e, Slot* sl, const BlockGeom& g, const uint32_t* d_seed, const uint32_t* ks,
+                  const uint32_t* kr, uint32_t flags, uint32_t* out, cudaStream_t s) {
+    uint32_t* hat = reinterpret_cast<uint32_t*>(sl->spec);
+    uint32_t* a = reinterpret_cast<uint32_t*>(sl->work);
+    uint32_t* tmp = reinterpret_cast<uint32_t*>(sl->work2);
+    int rc = pa::launch_exact_seed(g, d_seed, hat, tmp, &sl->ntt, s);
+    if (!rc) rc = pa::launch_exact_block(g, ks, kr, flags, hat, a, tmp, out, &sl->ntt, s);
+    return rc ? cuda_fail(e, (cudaError_t)rc) : PA_OK;
+}
+
+// Geometry of a job under the engine's split table, or under the split of its cached spectrum.
+int job_geom(pa_engine* e, Pool* p, const pa_job& j, BlockGeom* g) {
+    if (!j.key_start || !j.out) return PA_ERR_INVALID_ARG;
+    if ((j.flags & PA_FLAG_XOR_KEY_REST) && !j.key_rest) return PA_ERR_INVALID_ARG;
+    if (j.flags & PA_FLAG_EXACT) return PA_ERR_INVALID_ARG;
+    int rc = make_geom(j.n, j.v, j.flags, e->split, g);
+    if (rc) return rc;
+    if (g->exact_only || g->log_np > kFp32MaxLogNp) return PA_ERR_TOO_LARGE;
+    if (j.seed_id >= 0) {
+        if ((size_t)j.seed_id >= p->seeds.size() || !p->seeds[j.seed_id].live) return PA_ERR_NO_SEED;
+        const BlockGeom& sg = p->seeds[j.seed_id].g;
+        if (g->log_n1 && sg.log_n == g->log_n) {
+            g->log_n2 = sg.log_n2;
+            g->log_n1 = sg.log_n - sg.log_n2;
+        }
+        if (!same_seed_geom(sg, *g)) return PA_ERR_INVALID_ARG;
+    } else if (!j.seed_words) {
+        return PA_ERR_NO_SEED;
+    }
+    return PA_OK;
+}
+
+bool any_busy(Pool* p) {
+    for (Slot* sl : p->slots)
+        if (sl->busy) return true;
+    return false;
+}
+
+// Frees idle slots (least recently used first) until `need` more bytes fit the budget.
+bool make_room(Pool* p, size_t need) {
+    while (p->used + need > p->budget) {
+        Slot* victim = nullptr;
+        for (Slot* sl : p->slots)
+            if (!sl->busy && (!victim || sl->last_use < victim->last_use)) victim = sl;
+        if (!victim) return false;
+        p->slots.erase(std::find(p->slots.begin(), p->slots.end(), victim));
+        free_slot(p, victim);
+        drop_graphs(p);
+    }
+    return true;
+}
+
+uint64_t fnv(uint64_t h, const void* data, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(data);
+    for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    return h;
+}
+
+double job_cost(const BlockGeom& g, bool dynamic) {
+    const double np = double(1ull << g.log_np);
+    return np * g.log_np * (dynamic ? 1.6 : 1.0);
+}
+
+int batch_enqueue(pa_engine* e, Pool* p, const std::vector<std::vector<int>>& order, cudaStream_t s) {
+    PA_CUDA(e, cudaEventRecord(p->fork, s));
+    for (size_t k = 0; k < order.size(); ++k) {
+        Slot* sl = p->slots[k];
+        PA_CUDA(e, cudaStreamWaitEvent(sl->s, p->fork, 0));
+        for (int j : order[k]) {
+            const pa_job& jb = p->jobs[j];
+            const BlockGeom& g = p->geoms[j];
+            unsigned long long* cnt = p->job_cnt + 2 * (size_t)j;
+            unsigned int* resid = p->job_resid + j;
+            const float2* spec;
+            int rc;
+            if (jb.seed_id >= 0) {
+                const SeedEntry& se = p->seeds[jb.seed_id];
+                PA_CUDA(e, cudaMemcpyAsync(cnt + 1, se.cnt, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                                           sl->s));
+                spec = se.spec;
+            } else {
+                rc = seed_in_slot(e, sl, g, jb.seed_words, sl->spec, cnt + 1, sl->s);
+                if (rc) return rc;
+                spec = sl->spec;
+            }
+            rc = key_in_slot(e, sl, g, jb.key_start, jb.key_rest, jb.flags, spec, cnt, resid,
+                             reinterpret_cast<uint32_t*>(jb.out), sl->s);
+            if (rc) return rc;
+        }
+        PA_CUDA(e, cudaEventRecord(sl->join, sl->s));
+        PA_CUDA(e, cudaStreamWaitEvent(s, sl->join, 0));
+    }
+    return PA_OK;
+}
+
+}  // namespace
+
+void pool_destroy(pa_engine* e) {
+    Pool* p = e->pool;
+    if (!p) return;
+    drop_graphs(p);
+    for (Slot* sl : p->slots) free_slot(p, sl);
+    for (auto& se : p->seeds) {
+        cudaFree(se.spec);
+        cudaFree(se.seed);
+        cudaFree(se.cnt);
+    }
+    cudaFree(p->job_cnt);
+    cudaFree(p->job_resid);
+    if (p->fork) cudaEventDestroy(p->fork);
+    if (p->b0) cudaEventDestroy(p->b0);
+    if (p->b1) cudaEventDestroy(p->b1);
+    delete p;
+    e->pool = nullptr;
+}
+
+}  // namespace pa_host
+
+using namespace pa_host;
+
+extern "C" {
+
+int pa_set_pool(pa_engine* e, uint64_t hbm_budget_bytes, int32_t max_slots, int32_t batch_slots) {
+    if (!e || max_slots < 0 || batch_slots < 0 || max_slots > 256 || batch_slots > 256) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    Pool* p = get_pool(e);
+    if (!p) return PA_ERR_CUDA;
+    if (hbm_budget_bytes) p->budget = hbm_budget_bytes;
+    p->max_slots = max_slots ? max_slots : 16;
+    p->batch_slots = batch_slots ? batch_slots : 8;
+    drop_graphs(p);
+    return PA_OK;
+}
+
+int pa_seed_cache_add(pa_engine* e, const uint32_t* seed_words, uint32_t n, uint32_t v, uint32_t flags,
+                      int32_t* seed_id) {
+    if (!e || !seed_words || !seed_id) return PA_ERR_INVALID_ARG;
+    BlockGeom g;
+    int rc = make_geom(n, v, flags & ~PA_FLAG_EXACT, e->split, &g);
+    if (rc) return rc;
+    if (g.exact_only || g.log_np > kFp32MaxLogNp) return PA_ERR_TOO_LARGE;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    Pool* p = get_pool(e);
+    if (!p) return PA_ERR_CUDA;
+    if (any_busy(p) || p->batch_pending) return PA_ERR_BUSY;
+    SeedEntry se;
+    se.g = g;
+    const size_t words = n / 32u;
+    se.bytes = (size_t(1) << g.log_n) * sizeof(float2) + words * 4 + 8;
+    if (!make_room(p, se.bytes)) return PA_ERR_TOO_LARGE;
+    cudaError_t err = cudaMalloc(&se.spec, (size_t(1) << g.log_n) * sizeof(float2));
+    if (err == cudaSuccess) err = cudaMalloc(&se.seed, words * 4);
+    if (err == cudaSuccess) err = cudaMalloc(&se.cnt, sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaMemcpy(se.seed, seed_words, words * 4, cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) {
+        cudaFree(se.spec);
+        cudaFree(se.seed);
+        cudaFree(se.cnt);
+        return cuda_fail(e, err);
+    }
+    // build in any idle slot large enough (or a temporary one)
+    Slot* sl = nullptr;
+    for (Slot* c : p->slots)
+        if (!c->busy && c->cap >= g.log_np && (!sl || c->cap < sl->cap)) sl = c;
+    Slot* tmp = nullptr;
+    if (!sl) {
+        if (!make_room(p, slot_bytes(g.log_np))) rc = PA_ERR_TOO_LARGE;
+        else rc = new_slot(e, p, g.log_np, &tmp);
+        sl = tmp;
+    }
+    if (!rc) rc = seed_in_slot(e, sl, g, se.seed, se.spec, se.cnt, sl->s);
+    if (!rc && cudaStreamSynchronize(sl->s) != cudaSuccess) rc = PA_ERR_CUDA;
+    int derr = 0;
+    if (!rc && cudaMemcpy(&derr, sl->err, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && derr) {
+        cudaMemset(sl->err, 0, sizeof(int));
+        e->last_cuda = (int)cudaErrorLaunchTimeout;
+        rc = PA_ERR_CUDA;
+    }
+    if (tmp) {
+        if ((int)p->slots.size() < p->max_slots) {  // keep it: blocks of this size will want it
+            tmp->last_use = ++p->clock;
+            p->slots.push_back(tmp);
+        } else {
+            free_slot(p, tmp);
+        }
+    }
+    if (rc) {
+        cudaFree(se.spec);
+        cudaFree(se.seed);
+        cudaFree(se.cnt);
+        return rc;
+    }
+    se.live = true;
+    p->used += se.bytes;
+    p->seeds.push_back(se);
+    *seed_id = (int32_t)(p->seeds.size() - 1);
+    return PA_OK;
+}
+
+int pa_seed_cache_clear(pa_engine* e) {
+    if (!e) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    Pool* p = e->pool;
+    if (!p) return PA_OK;
+    if (any_busy(p) || p->batch_pending) return PA_ERR_BUSY;
+    drop_graphs(p);
+    for (auto& se : p->seeds) {
+        cudaFree(se.spec);
+        cudaFree(se.seed);
+        cudaFree(se.cnt);
+        p->used -= std::min(p->used, se.bytes);
+    }
+    p->seeds.clear();
+    return PA_OK;
+}
+
+int pa_batch_run(pa_engine* e, const pa_job* jobs, uint32_t count, uint32_t batch_flags, void* stream) {
+    if (!e || (!jobs && count)) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    Pool* p = get_pool(e);
+    if (!p) return PA_ERR_CUDA;
+    if (any_busy(p) || p->batch_pending) return PA_ERR_BUSY;
+    std::vector<BlockGeom> geoms(count);
+    int need_cap = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        int rc = job_geom(e, p, jobs[i], &geoms[i]);
+        if (rc) return rc;
+        if (reinterpret_cast<uintptr_t>(jobs[i].out) & 3u) return PA_ERR_INVALID_ARG;
+        need_cap = std::max(need_cap, geoms[i].log_np);
+    }
+    cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+    p->batch_stream = s;
+    p->jobs.assign(jobs, jobs + count);
+    p->geoms = geoms;
+    if (count == 0) {
+        PA_CUDA(e, cudaEventRecord(p->b0, s));
+        PA_CUDA(e, cudaEventRecord(p->b1, s));
+        p->batch_pending = true;
+        return PA_OK;
+    }
+    int K = (batch_flags & PA_BATCH_SERIAL) ? 1 : std::min<int>(p->batch_slots, (int)count);
+    K = std::min(K, p->max_slots);
+    // slots 0..K-1 must hold the largest block of the batch
+    for (int k = 0; k < K; ++k) {
+        if (k < (int)p->slots.size() && p->slots[k]->cap >= need_cap) continue;
+        if (k < (int)p->slots.size()) {
+            Slot* old = p->slots[k];
+            p->slots.erase(p->slots.begin() + k);
+            free_slot(p, old);
+            drop_graphs(p);
+        }
+        Slot* sl = nullptr;
+        // free idle slots beyond K first, then give up on parallelism if HBM is short
+        while (p->used + slot_bytes(need_cap) > p->budget && (int)p->slots.size() > k) {
+            Slot* victim = p->slots.back();
+            p->slots.pop_back();
+            free_slot(p, victim);
+            drop_graphs(p);
+        }
+        if (p->used + slot_bytes(need_cap) > p->budget) {
+            if (k == 0) return PA_ERR_TOO_LARGE;
+            K = k;
+            break;
+        }
+        int rc = new_slot(e, p, need_cap, &sl);
+        if (rc) return rc;
+        p->slots.insert(p->slots.begin() + k, sl);
+    }
+    if (p->job_cap < count) {
+        cudaFree(p->job_cnt);
+        cudaFree(p->job_resid);
+        p->job_cnt = nullptr;
+        p->job_resid = nullptr;
+        p->job_cap = 0;
+        drop_graphs(p);
+        PA_CUDA(e, cudaMalloc(&p->job_cnt, (size_t)count * 2 * sizeof(unsigned long long)));
+        PA_CUDA(e, cudaMalloc(&p->job_resid, (size_t)count * sizeof(unsigned int)));
+        p->job_cap = count;
+    }
+    // longest job first onto the least-loaded slot
+    std::vector<int> idx(count);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::vector<double> cost(count);
+    for (uint32_t i = 0; i < count; ++i) cost[i] = job_cost(geoms[i], jobs[i].seed_id < 0);
+    if (!(batch_flags & PA_BATCH_SERIAL))
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<std::vector<int>> order(K);
+    std::vector<double> load(K, 0.0);
+    p->job_slot.assign(count, 0);
+    for (int j : idx) {
+        int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        order[k].push_back(j);
+        load[k] += cost[j];
+        p->job_slot[j] = k;
+    }
+    for (int k = 0; k < K; ++k) p->slots[k]->last_use = ++p->clock;
+    PA_CUDA(e, cudaEventRecord(p->b0, s));
+    if (batch_flags & PA_BATCH_GRAPH) {
+        uint64_t key = fnv(1469598103934665603ull, jobs, sizeof(pa_job) * count);
+        key = fnv(key, &K, sizeof(K));
+        key = fnv(key, &batch_flags, sizeof(batch_flags));
+        for (const auto& g : geoms) key = fnv(key, &g, sizeof(g));
+        auto it = p->graphs.find(key);
+        if (it == p->graphs.end()) {
+            PA_CUDA(e, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+            int rc = batch_enqueue(e, p, order, s);
+            cudaGraph_t graph = nullptr;
+            cudaError_t cerr = cudaStreamEndCapture(s, &graph);
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (cerr != cudaSuccess) return cuda_fail(e, cerr);
+            cudaGraphExec_t exec = nullptr;
+            cerr = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (cerr != cudaSuccess) return cuda_fail(e, cerr);
+            if (p->graphs.size() >= 16) drop_graphs(p);
+            it = p->graphs.emplace(key, exec).first;
+        }
+        PA_CUDA(e, cudaGraphLaunch(it->second, s));
+    } else {
+        int rc = batch_enqueue(e, p, order, s);
+        if (rc) return rc;
+    }
+    PA_CUDA(e, cudaEventRecord(p->b1, s));
+    p->batch_pending = true;
+    return PA_OK;
+}
+
+int pa_batch_sync(pa_engine* e, pa_stats* stats, uint32_t count) {
+    if (!e) return PA_ERR_INVALID_ARG;
+    Pool* p = e->pool;
+    if (!p || !p->batch_pending) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    p->batch_pending = false;
+    PA_CUDA(e, cudaStreamSynchronize(p->batch_stream));
+    const uint32_t nj = (uint32_t)p->jobs.size();
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->b0, p->b1);
+    for (Slot* sl : p->slots) {
+        int derr = 0;
+        PA_CUDA(e, cudaMemcpy(&derr, sl->err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (derr) {  // a bounded device wait expired: results of this batch are not valid
+            cudaMemset(sl->err, 0, sizeof(int));
+            e->last_cuda = (int)cudaErrorLaunchTimeout;
+            return PA_ERR_CUDA;
+        }
+    }
+    if (nj == 0) return PA_OK;
+    std::vector<unsigned long long> cnt(2 * (size_t)nj);
+    std::vector<unsigned int> rb(nj);
+    PA_CUDA(e, cudaMemcpy(cnt.data(), p->job_cnt, cnt.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    PA_CUDA(e, cudaMemcpy(rb.data(), p->job_resid, rb.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost));
+    for (uint32_t j = 0; j < nj; ++j) {
+        float r;
+        std::memcpy(&r, &rb[j], sizeof(r));
+        int exact = 0;
+        if (!(r <= e->residual_limit)) {  // FP32 budget exceeded: recompute this block exactly
+            const pa_job& jb = p->jobs[j];
+            const uint32_t* seed = jb.seed_id >= 0 ? p->seeds[jb.seed_id].seed : jb.seed_words;
+            Slot* sl = p->slots[0];
+            int rc = exact_in_slot(e, sl, p->geoms[j], seed, jb.key_start, jb.key_rest, jb.flags,
+                                   reinterpret_cast<uint32_t*>(jb.out), sl->s);
+            if (rc) return rc;
+            PA_CUDA(e, cudaStreamSynchronize(sl->s));
+            exact = 1;
+        }
+        if (stats && j < count) {
+            stats[j].max_residual = r;
+            stats[j].popcount_key = cnt[2 * j];
+            stats[j].popcount_seed = cnt[2 * j + 1];
+            stats[j].gpu_ms = ms;
+            stats[j].seed_uses_left = -1;
+            stats[j].exact = exact;
+        }
+    }
+    return PA_OK;
+}
+
+int pa_submit(pa_engine* e, const pa_job* job, uint64_t* ticket) {
+    if (!e || !job || !ticket) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    Pool* p = get_pool(e);
+    if (!p) return PA_ERR_CUDA;
+    if (p->batch_pending) return PA_ERR_BUSY;
+    BlockGeom g;
+    int rc = job_geom(e, p, *job, &g);
+    if (rc) return rc;
+    // at most max_slots blocks in flight; the smallest idle slot that holds the block, else a new
+    // one within the budget (idle slots are freed, least recently used first, to make room)
+    int busy = 0;
+    for (Slot* c : p->slots) busy += c->busy ? 1 : 0;
+    if (busy >= p->max_slots) return PA_ERR_BUSY;
+    Slot* sl = nullptr;
+    for (Slot* c : p->slots)
+        if (!c->busy && c->cap >= g.log_np && (!sl || c->cap < sl->cap)) sl = c;
+    if (!sl) {
+        if ((int)p->slots.size() >= p->max_slots) {
+            Slot* victim = nullptr;
+            for (Slot* c : p->slots)
+                if (!c->busy && (!victim || c->last_use < victim->last_use)) victim = c;
+            if (!victim) return PA_ERR_BUSY;
+            p->slots.erase(std::find(p->slots.begin(), p->slots.end(), victim));
+            free_slot(p, victim);
+            drop_graphs(p);
+        }
+        if (!make_room(p, slot_bytes(g.log_np))) return any_busy(p) ? PA_ERR_BUSY : PA_ERR_TOO_LARGE;
+        rc = new_slot(e, p, g.log_np, &sl);
+        if (rc) return rc;
+        p->slots.push_back(sl);
+    }
+    const uint32_t n = job->n, v = job->v;
+    cudaStream_t s = sl->s;
+    const float2* spec;
+    if (job->seed_id >= 0) {
+        const SeedEntry& se = p->seeds[job->seed_id];
+        PA_CUDA(e, cudaMemcpyAsync(sl->cnt + 1, se.cnt, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s));
+        spec = se.spec;
+    } else {
+        PA_CUDA(e, cudaMemcpyAsync(sl->seed, job->seed_words, (size_t)(n / 32u) * 4u, cudaMemcpyHostToDevice, s));
+        rc = seed_in_slot(e, sl, g, sl->seed, sl->spec, sl->cnt + 1, s);
+        if (rc) return rc;
+        spec = sl->spec;
+    }
+    PA_CUDA(e, cudaMemcpyAsync(sl->ks, job->key_start, (size_t)(g.h / 32u + 1u) * 4u, cudaMemcpyHostToDevice, s));
+    if (job->flags & PA_FLAG_XOR_KEY_REST)
+        PA_CUDA(e, cudaMemcpyAsync(sl->kr, job->key_rest, (size_t)(v / 32u) * 4u, cudaMemcpyHostToDevice, s));
+    rc = key_in_slot(e, sl, g, sl->ks, sl->kr, job->flags, spec, sl->cnt, sl->resid, sl->out, s);
+    if (rc) return rc;
+    PA_CUDA(e, cudaMemcpyAsync(job->out, sl->out, pa_output_bytes(n, v, job->flags), cudaMemcpyDeviceToHost, s));
+    PA_CUDA(e, cudaMemcpyAsync(sl->host->cnt, sl->cnt, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    PA_CUDA(e, cudaMemcpyAsync(&sl->host->resid, sl->resid, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    PA_CUDA(e, cudaMemcpyAsync(&sl->host->err, sl->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PA_CUDA(e, cudaEventRecord(sl->done, s));
+    sl->busy = true;
+    sl->ticket = p->next_ticket++;
+    sl->job = *job;
+    sl->g = g;
+    sl->seed_id = job->seed_id;
+    sl->last_use = ++p->clock;
+    *ticket = sl->ticket;
+    return PA_OK;
+}
+
+int pa_poll(pa_engine* e, uint64_t ticket, pa_stats* stats) {
+    if (!e || !e->pool) return PA_ERR_INVALID_ARG;
+    Pool* p = e->pool;
+    Slot* sl = nullptr;
+    for (Slot* c : p->slots)
+        if (c->busy && c->ticket == ticket) sl = c;
+    if (!sl) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    cudaError_t q = cudaEventQuery(sl->done);
+    if (q == cudaErrorNotReady) return PA_PENDING;
+    if (q != cudaSuccess) {
+        sl->busy = false;
+        return cuda_fail(e, q);
+    }
+    const Mirror m = *sl->host;
+    if (m.err) {
+        cudaMemset(sl->err, 0, sizeof(int));
+        sl->busy = false;
+        e->last_cuda = (int)cudaErrorLaunchTimeout;
+        return PA_ERR_CUDA;
+    }
+    float r;
+    std::memcpy(&r, &m.resid, sizeof(r));
+    int exact = 0;
+    if (!(r <= e->residual_limit)) {  // FP32 budget exceeded: recompute exactly, then copy out again
+        const pa_job& jb = sl->job;
+        const uint32_t* seed = sl->seed_id >= 0 ? p->seeds[sl->seed_id].seed : sl->seed;
+        int rc = exact_in_slot(e, sl, sl->g, seed, sl->ks, sl->kr, jb.flags, sl->out, sl->s);
+        if (!rc && cudaMemcpyAsync(jb.out, sl->out, pa_output_bytes(jb.n, jb.v, jb.flags), cudaMemcpyDeviceToHost,
+                                   sl->s) != cudaSuccess)
+            rc = PA_ERR_CUDA;
+        if (!rc && cudaStreamSynchronize(sl->s) != cudaSuccess) rc = PA_ERR_CUDA;
+        if (rc) {
+            sl->busy = false;
+            return rc;
+        }
+        exact = 1;
+    }
+    if (stats) {
+        stats->max_residual = r;
+        stats->popcount_key = m.cnt[0];
+        stats->popcount_seed = m.cnt[1];
+        stats->gpu_ms = 0.f;
+        stats->seed_uses_left = -1;
+        stats->exact = exact;
+    }
+    sl->busy = false;
+    sl->last_use = ++p->clock;
+    return PA_OK;
+}
+
+int pa_set_split(pa_engine* e, uint32_t log_n, uint32_t log_n2) {
+    if (!e || log_n < 15 || log_n > 26) return PA_ERR_INVALID_ARG;
+    if ((int)log_n2 < split_min((int)log_n) || (int)log_n2 > split_max((int)log_n)) return PA_ERR_INVALID_ARG;
+    e->split[log_n] = (int8_t)log_n2;
+    e->spec_valid = false;  // the cached single-block spectrum may use the old layout
+    if (e->pool) drop_graphs(e->pool);
+    return PA_OK;
+}
+
+int pa_get_split(pa_engine* e, uint32_t log_n) {
+    if (!e || log_n < 15 || log_n > 26) return 0;
+    int l2 = e->split[log_n];
+    if (l2 < split_min((int)log_n) || l2 > split_max((int)log_n)) l2 = split_default((int)log_n);
+    return l2;
+}
+
+int pa_autotune(pa_engine* e, uint32_t min_n, uint32_t max_n, float* ms_out) {
+    if (!e || min_n < 1024u || max_n < min_n) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    Pool* p = get_pool(e);
+    if (!p) return PA_ERR_CUDA;
+    if (any_busy(p) || p->batch_pending) return PA_ERR_BUSY;
+    const int lo = std::max(15, ceil_log2(min_n) - 1), hi = std::min(26, ceil_log2(max_n) - 1);
+    if (ms_out)
+        for (int i = 0; i < 32; ++i) ms_out[i] = 0.f;
+    if (lo > hi) return PA_OK;
+    // one slot of the largest size times every candidate
+    const int cap = hi + 1;
+    Slot* sl = nullptr;
+    for (Slot* c : p->slots)
+        if (!c->busy && c->cap >= cap && (!sl || c->cap < sl->cap)) sl = c;
+    if (!sl) {
+        if (!make_room(p, slot_bytes(cap))) return PA_ERR_TOO_LARGE;
+        int rc = new_slot(e, p, cap, &sl);
+        if (rc) return rc;
+        p->slots.push_back(sl);
+    }
+    cudaStream_t s = sl->s;
+    const size_t words = (size_t(1) << cap) / 32;
+    PA_CUDA(e, cudaMemsetAsync(sl->seed, 0x5A, words * 4, s));  // data-independent timing: a fixed pattern
+    PA_CUDA(e, cudaMemsetAsync(sl->ks, 0xA5, words * 4, s));
+    PA_CUDA(e, cudaMemsetAsync(sl->kr, 0x3C, words * 4, s));
+    cudaEvent_t t0, t1;
+    PA_CUDA(e, cudaEventCreate(&t0));
+    PA_CUDA(e, cudaEventCreate(&t1));
+    int rc = PA_OK;
+    for (int ln = lo; ln <= hi && !rc; ++ln) {
+        const uint32_t n = 1u << (ln + 1), v = n / 4u + n / 8u;
+        float best = 0.f;
+        int best_l2 = split_default(ln);
+        for (int l2 = split_min(ln); l2 <= split_max(ln) && !rc; ++l2) {
+            int8_t tbl[32] = {};
+            tbl[ln] = (int8_t)l2;
+            BlockGeom g;
+            rc = make_geom(n, v, PA_FLAG_XOR_KEY_REST | PA_FLAG_COMPRESS, tbl, &g);
+            if (rc) break;
+            rc = seed_in_slot(e, sl, g, sl->seed, sl->spec, sl->cnt + 1, s);
+            float acc = 0.f;
+            const int reps = 3;
+            for (int r = 0; r <= reps && !rc; ++r) {  // first run warms up
+                if (cudaEventRecord(t0, s) != cudaSuccess) rc = PA_ERR_CUDA;
+                if (!rc) rc = key_in_slot(e, sl, g, sl->ks, sl->kr, PA_FLAG_XOR_KEY_REST | PA_FLAG_COMPRESS, sl->spec,
+                                          sl->cnt, sl->resid, sl->out, s);
+                if (!rc && cudaEventRecord(t1, s) != cudaSuccess) rc = PA_ERR_CUDA;
+                if (!rc && cudaEventSynchronize(t1) != cudaSuccess) rc = PA_ERR_CUDA;
+                float ms = 0.f;
+                if (!rc) cudaEventElapsedTime(&ms, t0, t1);
+                if (r) acc += ms;
+            }
+            if (rc) break;
+            const float ms = acc / reps;
+            if (best == 0.f || ms < best) {
+                best = ms;
+                best_l2 = l2;
+            }
+        }
+        if (!rc) {
+            e->split[ln] = (int8_t)best_l2;
+            if (ms_out) ms_out[ln] = best;
+        }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    int derr = 0;
+    if (cudaMemcpy(&derr, sl->err, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && derr) {
+        cudaMemset(sl->err, 0, sizeof(int));
+        e->last_cuda = (int)cudaErrorLaunchTimeout;
+        rc = PA_ERR_CUDA;
+    }
+    e->spec_valid = false;
+    drop_graphs(p);
+    return rc;
+}
+
+}  // extern "C"

@@ -3,8 +3,7 @@
 // Owns the HBM working set of one GPU (the reference's device buffers di1/di2/do1/do2 and its cuFFT
 // plans, PrivacyAmplification.cu:1567-1593, 1714-1751), the cached seed spectrum and the
 // reuse_seed_amount bookkeeping of the host loop (PrivacyAmplification.cu:1762-1797, 2099-2101).
-#include "../../include/pa_gb300.h"
-#include "pa_kernels.cuh"
+#include "pa_engine_impl.h"
 
 #include <cuda_runtime.h>
 
@@ -16,72 +15,14 @@
 #include <vector>
 
 using pa::BlockGeom;
+using pa_host::ceil_log2;
+using pa_host::cuda_fail;
+using pa_host::is_pow2;
 
-struct pa_engine {
-    int device = 0;
-    int num_sms = 0;
-    cudaStream_t stream = nullptr;
-    uint32_t max_n = 0;
-    int cap_log_np = 0;  // largest cyclic length the buffers hold
-    float residual_limit = 0.25f;
-    // HBM working set
-    uint32_t* d_key_start = nullptr;
-    uint32_t* d_key_rest = nullptr;
-    uint32_t* d_seed = nullptr;
-    uint32_t* d_out = nullptr;
-    float2* d_work = nullptr;   // pass A output (row-major)
-    float2* d_work2 = nullptr;  // pass B output (tile-major)
-    float2* d_spec = nullptr;
-    int* d_err = nullptr;       // device error word of the bounded TMA waits
-    uint32_t* d_exact_seed = nullptr;  // NTT of the placed seed (exact path), Np words
-    pa::NttTables* ntt = nullptr;      // exact-path twiddle tables
-    bool exact_valid = false;          // d_exact_seed matches the current seed for exact_geom
-    bool last_exact = false;           // the last block ran on the exact path
-    BlockGeom exact_geom{};
-    pa::PassMaps maps{};        // tensor maps for the geometry maps_log_n
-    int maps_log_n = -1;
-    uint32_t* d_planes = nullptr;
-    unsigned long long* d_cnt = nullptr;  // [0] key popcount, [1] seed popcount
-    unsigned int* d_resid = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // seed state
-    bool seed_valid = false;
-    uint32_t seed_n = 0;
-    int64_t seed_left = 0;  // -1 = unlimited
-    bool spec_valid = false;
-    BlockGeom spec_geom{};
-    int last_cuda = 0;
-    bool pending = false;  // device-form work queued and not yet synchronised
-    // per-kernel timing ring (pa_set_timing / pa_stage_times)
-    bool timing = false;
-    std::vector<std::array<cudaEvent_t, 5>> tev;
-    std::vector<int> tev_stages;
-    size_t tev_next = 0, tev_count = 0;
-};
-
-namespace {
-
-int ceil_log2(uint64_t x) {
-    int l = 0;
-    while ((1ull << l) < x) ++l;
-    return l;
-}
-
-bool is_pow2(uint32_t x) { return x && !(x & (x - 1u)); }
-
-int cuda_fail(pa_engine* e, cudaError_t err) {
-    e->last_cuda = (int)err;
-    return PA_ERR_CUDA;
-}
-
-#define PA_CUDA(e, call)                                  \
-    do {                                                  \
-        cudaError_t err__ = (call);                       \
-        if (err__ != cudaSuccess) return cuda_fail(e, err__); \
-    } while (0)
+namespace pa_host {
 
 // Block geometry (sizes, padded cyclic length, three-pass split) for (n, v, flags).
-int make_geom(uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
+int make_geom(uint32_t n, uint32_t v, uint32_t flags, const int8_t* split, BlockGeom* g) {
     if (n < 1024u || (n & 31u) || (v & 31u) || v == 0 || v >= n) return PA_ERR_INVALID_ARG;
     g->n = n;
     g->v = v;
@@ -101,7 +42,9 @@ int make_geom(uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
     if (g->log_n <= 14) {
         g->log_n1 = g->log_n2 = 0;
     } else if (g->log_n <= 26) {
-        g->log_n2 = std::min(14, g->log_n - 5);  // rows 2^10..2^14, columns 2^5..2^12
+        int l2 = split ? split[g->log_n] : 0;
+        if (l2 < split_min(g->log_n) || l2 > split_max(g->log_n)) l2 = split_default(g->log_n);
+        g->log_n2 = l2;  // rows 2^10..2^14, columns 2^5..2^12
         g->log_n1 = g->log_n - g->log_n2;
     } else {  // beyond the FP32 path: exact NTT only
         g->log_n1 = g->log_n2 = 0;
@@ -112,16 +55,23 @@ int make_geom(uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
 }
 
 bool same_seed_geom(const BlockGeom& a, const BlockGeom& b) {
-    if (a.log_np != b.log_np || a.n != b.n) return false;
+    if (a.log_np != b.log_np || a.n != b.n || a.log_n2 != b.log_n2) return false;
     if (is_pow2(a.n)) return true;  // placement is the identity
     return a.seed_direct == b.seed_direct && a.h == b.h;
 }
 
+}  // namespace pa_host
+
+namespace {
+
+using pa_host::make_geom;
+using pa_host::same_seed_geom;
+
 int ensure_maps(pa_engine* e, const BlockGeom& g) {
-    if (g.log_n1 == 0 || e->maps_log_n == g.log_n) return PA_OK;
+    if (g.log_n1 == 0 || e->maps_key == pa_host::maps_key(g)) return PA_OK;
     int rc = pa::make_pass_maps(g, e->d_work, e->d_work2, &e->maps);
     if (rc) return cuda_fail(e, (cudaError_t)rc);
-    e->maps_log_n = g.log_n;
+    e->maps_key = pa_host::maps_key(g);
     return PA_OK;
 }
 
@@ -154,7 +104,7 @@ int seed_common(pa_engine* e, uint32_t n, int32_t reuse, cudaStream_t s) {
     e->exact_valid = false;
     if (is_pow2(n)) {  // placement does not depend on v: build the spectrum now
         BlockGeom g;
-        int rc = make_geom(n, n / 2u, PA_FLAG_COMPRESS, &g);
+        int rc = make_geom(n, n / 2u, PA_FLAG_COMPRESS, e->split, &g);
         if (rc) return rc;
         return build_spectrum(e, g, s);
     }
@@ -251,7 +201,7 @@ size_t pa_output_bytes(uint32_t n, uint32_t v, uint32_t flags) {
 
 int pa_kernels_per_block(uint32_t n, uint32_t v, uint32_t flags) {
     BlockGeom g;
-    if (make_geom(n, v, flags, &g)) return 0;
+    if (make_geom(n, v, flags, nullptr, &g)) return 0;
     if (g.exact_only || (flags & PA_FLAG_EXACT)) return pa::exact_kernel_count(g);
     return pa::kernel_count_key_block(g);
 }
@@ -262,8 +212,10 @@ const char* pa_error_string(int code) {
         case PA_ERR_INVALID_ARG: return "invalid argument";
         case PA_ERR_CUDA: return "CUDA error";
         case PA_ERR_NO_SEED: return "no seed set or reuse_seed_amount used up";
-        case PA_ERR_TOO_LARGE: return "block larger than the engine's max_sample_size";
+        case PA_ERR_TOO_LARGE: return "block larger than the engine or the pool can hold";
         case PA_ERR_PRECISION: return "FP32 residual above the precision limit";
+        case PA_ERR_BUSY: return "no slot or HBM free for the block now";
+        case PA_PENDING: return "block still running";
         default: return "unknown error";
     }
 }
@@ -321,6 +273,7 @@ void pa_destroy(pa_engine* e) {
     if (!e) return;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
+    pa_host::pool_destroy(e);
     cudaFree(e->d_key_start);
     cudaFree(e->d_key_rest);
     cudaFree(e->d_seed);
@@ -343,7 +296,7 @@ void pa_destroy(pa_engine* e) {
 }
 
 static int check_n(pa_engine* e, uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
-    int rc = make_geom(n, v, flags, g);
+    int rc = make_geom(n, v, flags, e->split, g);
     if (rc) return rc;
     if (n > e->max_n || g->log_np > e->cap_log_np) return PA_ERR_TOO_LARGE;
     return PA_OK;

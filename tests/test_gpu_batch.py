@@ -1,0 +1,139 @@
+"""Slot pool through the C ABI: every three-pass split, batched uneven mixes (serial, concurrent, CUDA
+graph) and the served form (pa_submit / pa_poll) -- each block bit-exact with the same block alone."""
+import numpy as np
+import pytest
+
+import privacyamplification_gb300 as pa
+from privacyamplification_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DEFAULT = pa.FLAG_XOR_KEY_REST | pa.FLAG_COMPRESS
+
+
+@pytest.fixture(scope="module")
+def torch_cuda(pa_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("a GPU test ran without a CUDA device")
+    return torch
+
+
+@pytest.fixture()
+def engine(pa_lib):
+    eng = pa.Engine(max_sample_size=1 << 25)
+    yield eng
+    eng.close()
+
+
+@pytest.mark.parametrize("log_n", [15, 17, 19, 21, 22, 24])
+def test_every_split_matches_oracle(engine, log_n):
+    n = 1 << (log_n + 1)
+    v = n // 4 + n // 8
+    seed, recv = O.random_block(n, v, 77 + log_n)
+    ks, kr = O.key_split(recv, n, v)
+    ref = O.ntt(seed, ks, kr, n, v)
+    lo, hi = max(10, log_n - 12), min(14, log_n - 5)
+    for l2 in range(lo, hi + 1):
+        engine.set_split(log_n, l2)
+        assert engine.get_split(log_n) == l2
+        engine.set_seed(seed, n, -1)
+        assert np.array_equal(engine.process(ks, kr, n, v), ref), l2
+
+
+def test_split_rejects_out_of_range(engine):
+    with pytest.raises(pa.PAError):
+        engine.set_split(20, 15)
+    with pytest.raises(pa.PAError):
+        engine.set_split(20, 7)
+
+
+def alone(engine, seed, ks, kr, n, v, flags):
+    engine.set_seed(seed, n, -1)
+    return engine.process(ks, kr, n, v, flags)
+
+
+def small_mix():
+    blocks = W.uneven_mix(count=24, lo=12, hi=20, rng_seed=0xBEE)
+    blocks[3].flags = 0                      # no XOR, no compression (n/16 output bytes)
+    blocks[5].flags = pa.FLAG_COMPRESS       # compression without XOR
+    return blocks
+
+
+def test_batch_modes_match_alone(torch_cuda, engine):
+    blocks = small_mix()
+    mix = W.DeviceMix(engine, blocks)
+    want = [alone(engine, mix.seed_words(b), mix.key_start(b), mix.key_rest(b), b.n, b.v, b.flags) for b in blocks]
+    for i, b in enumerate(blocks[:6]):
+        if b.n <= 1 << 16:
+            assert np.array_equal(want[i], O.direct(mix.seed_words(b), mix.key_start(b), mix.key_rest(b), b.n, b.v,
+                                                    b.flags)), i
+    for mode in (pa.BATCH_SERIAL, 0, pa.BATCH_GRAPH, pa.BATCH_GRAPH):  # graph twice: capture, then replay
+        mix.d_out.zero_()
+        stats = mix.run(mode)
+        got = mix.outputs()
+        for i in range(len(blocks)):
+            assert np.array_equal(got[i], want[i]), (mode, i, blocks[i])
+        assert all(s.max_residual < 0.25 and s.exact == 0 for s in stats)
+
+
+def test_batch_after_autotune(torch_cuda, engine):
+    tuned = engine.autotune(1 << 16, 1 << 21)
+    assert set(tuned) == set(range(15, 21))
+    for ln, (l2, ms) in tuned.items():
+        assert max(10, ln - 12) <= l2 <= min(14, ln - 5) and ms > 0
+    blocks = small_mix()
+    mix = W.DeviceMix(engine, blocks)  # spectra cached with the tuned splits
+    want = [alone(engine, mix.seed_words(b), mix.key_start(b), mix.key_rest(b), b.n, b.v, b.flags) for b in blocks]
+    mix.run(pa.BATCH_GRAPH)
+    assert all(np.array_equal(g, w) for g, w in zip(mix.outputs(), want))
+
+
+def test_batch_guard_recomputes_exactly(torch_cuda, engine):
+    """A run-structured block (FP32 budget exceeded at n = 2^22) inside a batch comes back exact."""
+    n, v = 1 << 22, (1 << 20) + (1 << 19)
+    seed = np.zeros(n // 32, np.uint32)
+    seed[: n // 64] = 0xFFFFFFFF
+    recv = np.full(n // 32 + 1, 0xFFFFFFFF, np.uint32)
+    ks, kr = O.key_split(recv, n, v)
+    dev = torch_cuda.device("cuda")
+    t = lambda a: torch_cuda.from_numpy(np.ascontiguousarray(a).view(np.int32)).to(dev)
+    d_seed, d_ks, d_kr = t(seed), t(ks), t(kr)
+    d_out = torch_cuda.zeros(v // 8, dtype=torch_cuda.uint8, device=dev)
+    job = pa.PAJob(d_seed.data_ptr(), -1, d_ks.data_ptr(), d_kr.data_ptr(), n, v, DEFAULT, d_out.data_ptr())
+    engine.batch_run([job])
+    st = engine.batch_sync(1)[0]
+    assert st.max_residual > 0.25 and st.exact == 1
+    assert np.array_equal(d_out.cpu().numpy(), O.ntt(seed, ks, kr, n, v))
+
+
+def test_served_requests_match_alone(torch_cuda, engine):
+    """Poisson arrivals faster than the GPU drains them: blocks overlap, queue and are admitted as slots
+    free up; every result equals the same request alone."""
+    reqs = W.poisson_requests(rate=4000, count=48, lo=14, hi=20, rng_seed=11)
+    words = max(r.n // 32 + max(r.seed_word0, r.key_word0) for r in reqs) + 64
+    banks = W.HostBanks(words)
+    engine.set_pool(max_slots=4)
+    res = W.serve(engine, reqs, banks, out_slots=6, keep=lambda r: True)
+    assert len(res.latency_ms) == len(reqs) and res.exact == 0
+    for r in reqs:
+        want = alone(engine, banks.seed_words(r), banks.key_start(r), banks.key_rest(r), r.n, r.v, r.flags)
+        assert np.array_equal(res.outputs[r.rid], want), r
+
+
+def test_served_static_seeds_and_busy(torch_cuda, engine):
+    """Static (cached) seeds per power-of-two size; a budget of one slot forces PA_ERR_BUSY admission."""
+    reqs = W.poisson_requests(rate=2000, count=16, lo=14, hi=18, static=True, rng_seed=12)
+    words = max(r.n // 32 + max(r.seed_word0, r.key_word0) for r in reqs) + 64
+    banks = W.HostBanks(words)
+    seed_ids = {}
+    for r in reqs:
+        if (r.n, r.v, r.flags) not in seed_ids:
+            seed_ids[(r.n, r.v, r.flags)] = engine.seed_cache_add(banks.seed_words(r), r.n, r.v, r.flags)
+    engine.set_pool(max_slots=1)
+    res = W.serve(engine, reqs, banks, out_slots=4, keep=lambda r: True, seed_ids=seed_ids)
+    assert len(res.latency_ms) == len(reqs)
+    for r in reqs:
+        want = alone(engine, banks.seed_words(r), banks.key_start(r), banks.key_rest(r), r.n, r.v, r.flags)
+        assert np.array_equal(res.outputs[r.rid], want), r
