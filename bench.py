@@ -400,6 +400,184 @@ def run_ours(args):
     return 0
 
 
+# ------------------------------------------------------------------------------------ other workloads
+def _line(metric, value, unit, steps, warmup, ms_per_step, workload, extra, higher=True):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": higher, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": DATA, "config": {"workload": workload}}
+    line.update(extra)
+    print(json.dumps(line))
+
+
+def run_dynamic27(args):
+    """Precision-stress size with a fresh seed per block: seed spectrum + key block, n = 2^27."""
+    import numpy as np
+    import torch
+    import privacyamplification_gb300 as pa
+    from oracle.oracle import random_block
+    pa.load_library()
+    dev = torch.device("cuda", 0)
+    eng = pa.Engine(max_sample_size=N_BITS)
+    seeds, keys = [], []
+    for i in range(KEY_BUFFERS):
+        sd, recv = random_block(N_BITS, V_BITS, 0xD1 + i)
+        ks, kr = pa.key_split(recv, N_BITS, V_BITS)
+        seeds.append(torch.from_numpy(sd.view(np.int32)).to(dev))
+        keys.append((torch.from_numpy(ks.view(np.int32)).to(dev), torch.from_numpy(kr.view(np.int32)).to(dev)))
+    d_out = torch.empty(V_BITS // 32, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    def block(i):
+        eng.set_seed_device(seeds[i % len(seeds)].data_ptr(), N_BITS, 1, stream=stream.cuda_stream)
+        ks, kr = keys[i % len(keys)]
+        eng.process_device(ks.data_ptr(), kr.data_ptr(), N_BITS, V_BITS, d_out.data_ptr(), stream=stream.cuda_stream)
+
+    for i in range(args.warmup):
+        block(i)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record(stream)
+        for i in range(args.steps):
+            block(i)
+        ev1.record(stream)
+        ev1.synchronize()
+    st = eng.sync(check=False)
+    t = ev0.elapsed_time(ev1) / 1e3
+    _line(METRIC, args.steps * N_BITS / t / 1e9, UNIT, args.steps, args.warmup, t / args.steps * 1e3,
+          "n=2^27 (h=83886080, v=50331648), dynamic seed: a fresh seed spectrum every block, do_xor, do_compress",
+          {"max_residual": st.max_residual, "clocks": clk.summary(),
+           "gpu_launches": args.steps * (3 + pa.kernels_per_block(N_BITS, V_BITS))})
+    eng.close()
+
+
+def run_exact29(args):
+    """n = 2^29 (beyond the FP32 path): exact NTT path, fresh seed per block."""
+    import numpy as np
+    import torch
+    import privacyamplification_gb300 as pa
+    n = 1 << 29
+    v = n // 4 + n // 8
+    pa.load_library()
+    dev = torch.device("cuda", 0)
+    eng = pa.Engine(max_sample_size=n)
+    rng = np.random.default_rng(29)
+    words = lambda k: rng.integers(0, 1 << 32, size=k, dtype=np.uint64).astype(np.uint32)
+    seeds = [torch.from_numpy(words(n // 32).view(np.int32)).to(dev) for _ in range(2)]
+    ks = torch.from_numpy(words(n // 32).view(np.int32)).to(dev)
+    kr = torch.from_numpy(words(v // 32).view(np.int32)).to(dev)
+    d_out = torch.empty(v // 32, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    def block(i):
+        eng.set_seed_device(seeds[i % 2].data_ptr(), n, 1, stream=stream.cuda_stream)
+        eng.process_device(ks.data_ptr(), kr.data_ptr(), n, v, d_out.data_ptr(), stream=stream.cuda_stream)
+
+    for i in range(args.warmup):
+        block(i)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record(stream)
+        for i in range(args.steps):
+            block(i)
+        ev1.record(stream)
+        ev1.synchronize()
+    st = eng.sync(check=False)
+    t = ev0.elapsed_time(ev1) / 1e3
+    _line(METRIC, args.steps * n / t / 1e9, UNIT, args.steps, args.warmup, t / args.steps * 1e3,
+          "n=2^29 (h=n/2+n/8, v=n/4+n/8), dynamic seed, exact NTT path mod 3*2^30+1",
+          {"exact": st.exact, "clocks": clk.summary(), "dtype": "u32 (mod p)"})
+    eng.close()
+
+
+def run_batch(args):
+    """Uneven mix: 512 blocks, n log-uniform in [2^18, 2^25], v/n ~ U[0.1, 0.9], half static seeds."""
+    import torch
+    import privacyamplification_gb300 as pa
+    from privacyamplification_gb300 import workloads as W
+    pa.load_library()
+    eng = pa.Engine(max_sample_size=1 << 25)
+    t = time.perf_counter()
+    tuned = eng.autotune(1 << 18, 1 << 26)
+    tune_s = time.perf_counter() - t
+    blocks = W.uneven_mix()
+    mix = W.DeviceMix(eng, blocks)
+    bits = sum(b.n for b in blocks)
+    res = {}
+    for name, flags in (("serial", pa.BATCH_SERIAL), ("concurrent", 0), ("graph", pa.BATCH_GRAPH)):
+        for _ in range(args.warmup):
+            mix.run(flags)
+        ms = []
+        with ClockSampler(0) as clk:
+            for _ in range(args.steps):
+                st = mix.run(flags)
+                ms.append(st[0].gpu_ms)
+        res[name] = {"gbit_s": bits / (statistics.median(ms) / 1e3) / 1e9, "ms_median": statistics.median(ms),
+                     "ms_max": max(ms), "max_residual": max(x.max_residual for x in st),
+                     "exact_recomputed": sum(x.exact for x in st), "clocks": clk.summary()}
+    out_graph = mix.outputs()
+    mix.run(pa.BATCH_SERIAL)
+    same = all((a == b).all() for a, b in zip(out_graph, mix.outputs()))
+    g = res["graph"]
+    _line(METRIC, g["gbit_s"], UNIT, args.steps, args.warmup, g["ms_median"],
+          "uneven mix: 512 blocks, n log-uniform [2^18, 2^25] (multiple of 1024), v/n ~ U[0.1,0.9] (multiple "
+          "of 128), even blocks static seed (cached spectrum), odd blocks dynamic; one batch per step",
+          {"batch_bits": bits, "modes": res, "graph_vs_serial": g["gbit_s"] / res["serial"]["gbit_s"],
+           "graph_equals_serial": bool(same), "autotune_s": tune_s,
+           "splits": {str(k): v[0] for k, v in tuned.items()}, "clocks": g["clocks"]})
+    eng.close()
+
+
+def run_serve(args, static):
+    """Poisson arrivals; p50/p99 latency and sustained Gbit/s per rate; sampled same-alone-vs-in-mix check."""
+    import privacyamplification_gb300 as pa
+    from privacyamplification_gb300 import workloads as W
+    pa.load_library()
+    eng = pa.Engine(max_sample_size=1 << 27)
+    rates = [(10, 100), (100, 400), (500, 1000), (2000, 2000)]
+    all_reqs = {rate: W.poisson_requests(rate, count, static=static, rng_seed=rate) for rate, count in rates}
+    words = max(r.n // 32 + max(r.seed_word0, r.key_word0) for rs in all_reqs.values() for r in rs) + 64
+    banks = W.HostBanks(words)
+    seed_ids = None
+    if static:
+        seed_ids = {}
+        for rs in all_reqs.values():
+            for r in rs:
+                if W.seed_key(r.n, r.v, r.flags) not in seed_ids:
+                    seed_ids[W.seed_key(r.n, r.v, r.flags)] = eng.seed_cache_add(banks.seed_words(r), r.n, r.v, r.flags)
+    warm = W.poisson_requests(5000, 24, static=static, rng_seed=1)
+    for r in warm:
+        r.seed_word0 = r.key_word0 = 0
+        if static and W.seed_key(r.n, r.v, r.flags) not in seed_ids:
+            seed_ids[W.seed_key(r.n, r.v, r.flags)] = eng.seed_cache_add(banks.seed_words(r), r.n, r.v, r.flags)
+    W.serve(eng, warm, banks, seed_ids=seed_ids)
+    lines = []
+    checked = mismatched = 0
+    for rate, count in rates:
+        reqs = all_reqs[rate]
+        with ClockSampler(0) as clk:
+            res = W.serve(eng, reqs, banks, keep=lambda r: r.rid % 50 == 7, seed_ids=seed_ids)
+        for r in reqs:
+            if r.rid in res.outputs:
+                eng.set_seed(banks.seed_words(r), r.n, -1)
+                alone = eng.process(banks.key_start(r), banks.key_rest(r), r.n, r.v, r.flags)
+                checked += 1
+                mismatched += int(not (alone == res.outputs[r.rid]).all())
+        offered = sum(r.n for r in reqs) / reqs[-1].arrival / 1e9
+        lines.append({"rate_per_s": rate, "requests": count, "p50_ms": res.pct(50), "p99_ms": res.pct(99),
+                      "sustained_gbit_s": res.bits / res.wall_s / 1e9, "offered_gbit_s": offered,
+                      "wall_s": res.wall_s, "exact_recomputed": res.exact, "clocks": clk.summary()})
+    top = lines[-1]
+    _line("p99 latency", top["p99_ms"], "ms", len(rates), 1, None,
+          "serving: Poisson arrivals at 10/100/500/2000 blocks/s, n log-uniform [2^20, 2^27] "
+          + ("rounded to a power of two, static seed spectra cached per size" if static
+             else "(multiple of 1024), each request with its own seed")
+          + ", v/n ~ U[0.2,0.8]; continuous admission to slots",
+          {"rates": lines, "mix_equals_alone": {"checked": checked, "mismatched": mismatched}}, higher=False)
+    eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -408,11 +586,22 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT pipeline baseline leg")
+    ap.add_argument("--workload", default="static27",
+                    choices=["static27", "dynamic27", "exact29", "batch", "serve", "serve-static"],
+                    help="static27 (default): the headline line; the others print their own line")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "dynamic27":
+        return run_dynamic27(args)
+    if args.workload == "exact29":
+        return run_exact29(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload in ("serve", "serve-static"):
+        return run_serve(args, static=args.workload == "serve-static")
     return run_ours(args)
 
 

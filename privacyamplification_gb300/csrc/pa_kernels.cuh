@@ -21,13 +21,17 @@ struct BlockGeom {
 // Seed placement in the cyclic length Np.  For Np == n this is the identity.  For a padded Np the
 // outputs i < out_bits see exactly the reference's seed[(i-j) mod n] when
 //   s'[x] = s[x]               for x < seed_direct = min(Np - h, n),
-//   s'[x] = s[x - (Np - n)]    for x >= Np - h,
-//   s'[x] = 0                  otherwise.
+//   s'[x] = s[x - (Np - n)]    for x >= Np - h.
+// Positions in between (present when n + h < Np) are read by no output i < out_bits; they are filled
+// with seed bits s[x - seed_direct] (an index below n) rather than zeros: a long run of zeros would
+// give the placed seed large near-DC spectral coefficients and cost the FP32 path most of its
+// rounding budget.
 __host__ __device__ inline int seed_source(const BlockGeom& g, uint64_t x, uint64_t* src) {
     uint64_t np = 1ull << g.log_np;
     if (x < g.seed_direct) { *src = x; return 1; }
     if (x >= np - g.h) { *src = x - (np - g.n); return 1; }
-    return 0;
+    *src = x - g.seed_direct;
+    return 1;
 }
 
 }  // namespace pa

@@ -37,6 +37,12 @@ class Block:
         return self.n - self.v
 
 
+def seed_key(n, v, flags):
+    """Blocks that can share one cached seed spectrum: a power-of-two n places the seed identically for
+    every v and flags; otherwise the placement depends on h and the output length."""
+    return (n,) if n & (n - 1) == 0 else (n, v, flags)
+
+
 def _round_n(x, quantum=1024):
     return max(quantum, int(round(x / quantum)) * quantum)
 
@@ -91,7 +97,7 @@ class DeviceMix:
         self.seed_ids = {}
         for b in blocks:
             if b.static:
-                key = (b.n, b.v, b.flags)
+                key = seed_key(b.n, b.v, b.flags)
                 if key not in self.seed_ids:
                     self.seed_ids[key] = engine.seed_cache_add(self.seed_words(b), b.n, b.v, b.flags)
         torch.cuda.synchronize()
@@ -111,7 +117,7 @@ class DeviceMix:
 
     def _job(self, i, b):
         seed_ptr = 0 if b.static else self.d_seed.data_ptr() + 4 * b.seed_word0
-        sid = self.seed_ids[(b.n, b.v, b.flags)] if b.static else -1
+        sid = self.seed_ids[seed_key(b.n, b.v, b.flags)] if b.static else -1
         return PAJob(seed_ptr or None, sid, self.d_key.data_ptr() + 4 * b.key_word0,
                      self.d_rest.data_ptr() + 4 * b.key_word0, b.n, b.v, b.flags,
                      self.d_out.data_ptr() + int(self.out_off[i]))
@@ -212,7 +218,7 @@ def serve(engine, reqs, banks, out_slots=24, keep=lambda r: False, seed_ids=None
         while waiting and free_out:
             r = waiting[0]
             ob = free_out[-1]
-            sid = seed_ids[(r.n, r.v, r.flags)] if (r.static and seed_ids is not None) else -1
+            sid = seed_ids[seed_key(r.n, r.v, r.flags)] if (r.static and seed_ids is not None) else -1
             seed = None if sid >= 0 else banks.seed_words(r)
             job = PAJob(seed.ctypes.data if seed is not None else None, sid, banks.key_start(r).ctypes.data,
                         banks.key_rest(r).ctypes.data, r.n, r.v, r.flags, outs[ob].ctypes.data)

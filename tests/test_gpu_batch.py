@@ -129,8 +129,8 @@ def test_served_static_seeds_and_busy(torch_cuda, engine):
     banks = W.HostBanks(words)
     seed_ids = {}
     for r in reqs:
-        if (r.n, r.v, r.flags) not in seed_ids:
-            seed_ids[(r.n, r.v, r.flags)] = engine.seed_cache_add(banks.seed_words(r), r.n, r.v, r.flags)
+        if W.seed_key(r.n, r.v, r.flags) not in seed_ids:
+            seed_ids[W.seed_key(r.n, r.v, r.flags)] = engine.seed_cache_add(banks.seed_words(r), r.n, r.v, r.flags)
     engine.set_pool(max_slots=1)
     res = W.serve(engine, reqs, banks, out_slots=4, keep=lambda r: True, seed_ids=seed_ids)
     assert len(res.latency_ms) == len(reqs)

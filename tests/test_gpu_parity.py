@@ -170,3 +170,23 @@ def test_full_size_2p27_properties(gpu_engine):
         ref = O.direct(seed, ks1, kr1, n, v, pa.FLAG_COMPRESS, rows=(int(r0), int(r0) + 64))
         assert np.array_equal(o1[r0 // 8: r0 // 8 + 8], ref[r0 // 8: r0 // 8 + 8]), r0
     assert h == 83886080
+
+
+@pytest.mark.parametrize("n,v", [(2118656, 1371520), (4635648, 3624576), (9630720, 4456320), (17133568, 11170816)])
+def test_padded_nonpow2_stays_within_fp32_budget(gpu_engine, n, v):
+    """Non-power-of-two blocks whose padded cyclic length leaves a region no output reads (n + h < Np):
+    the FP32 path keeps its usual residual there, so no exact recompute is needed."""
+    seed, recv = O.random_block(n, v, n ^ v)
+    ks, kr = O.key_split(recv, n, v)
+    gpu_engine.set_seed(seed, n, -1)
+    out = gpu_engine.process(ks, kr, n, v)
+    st = gpu_engine.last_stats
+    assert st.exact == 0 and st.max_residual < 0.1, st.max_residual
+    if n <= 1 << 23:
+        assert np.array_equal(out, O.ntt(seed, ks, kr, n, v))
+    else:
+        blk = O.DirectBlock(seed, ks, n, v)
+        krb = O.bits_msb(kr, v).astype(np.uint8)
+        for r0 in (0, v // 2 // 64 * 64, v - 64):
+            assert np.array_equal(np.unpackbits(out[r0 // 8: r0 // 8 + 8]), blk.rows(r0, r0 + 64) ^ krb[r0: r0 + 64])
+        blk.close()
