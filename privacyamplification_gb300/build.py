@@ -17,7 +17,12 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpa_gb300.so")
 SOURCES = ["pa_kernels.cu", "pa_passes.cu", "pa_ntt.cu", "pa_engine.cu", "pa_batch.cu", "pa_noalloc.cu"]
-HEADERS = ["pa_device.cuh", "pa_fft.cuh", "pa_tma.cuh", "pa_kernels.cuh", "pa_engine_impl.h", os.path.join("..", "..", "include", "pa_gb300.h")]
+HOST_SOURCES = ["pa_sha3.cpp", "pa_config.cpp", "pa_zmtp.cpp", "pa_service.cpp"]  # plain C++, no CUDA
+SERVICE_MAIN = "pa_service_main.cpp"
+SERVICE = os.path.join(HERE, "pa_service")
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall"]
+HEADERS = ["pa_device.cuh", "pa_fft.cuh", "pa_tma.cuh", "pa_kernels.cuh", "pa_engine_impl.h",
+           os.path.join("..", "..", "include", "pa_gb300.h"), os.path.join("..", "..", "include", "pa_service.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
@@ -28,6 +33,13 @@ def nvcc() -> str:
         if c and os.path.exists(c):
             return c
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libpa_gb300.so")
+
+
+def cxx() -> str:
+    for c in (os.environ.get("CXX"), shutil.which("g++"), shutil.which("c++")):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("g++ not found: a C++17 compiler is required for the host loop")
 
 
 def _stale(target: str, deps) -> bool:
@@ -47,6 +59,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
             jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, "-c", s, "-o", o])
+    for src in HOST_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + hdrs):
+            jobs.append([cxx(), *CXX_FLAGS, "-c", s, "-o", o])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             results = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs))
@@ -61,6 +79,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
+    main = os.path.join(CSRC, SERVICE_MAIN)
+    if force or _stale(SERVICE, [LIB, main] + hdrs):
+        cmd = [cxx(), "-O2", "-std=c++17", main, "-o", SERVICE, "-L" + HERE, "-lpa_gb300", "-Wl,-rpath,$ORIGIN",
+               "-pthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("pa_service link failed")
     return LIB
 
 

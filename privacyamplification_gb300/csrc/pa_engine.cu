@@ -235,10 +235,8 @@ int pa_create(const pa_config* cfg, pa_engine** out) {
         delete e;
         return PA_ERR_TOO_LARGE;
     }
-    auto fail = [&](cudaError_t err) {
-        int code = (int)err;
+    auto fail = [&](cudaError_t) {
         pa_destroy(e);
-        (void)code;
         return PA_ERR_CUDA;
     };
     cudaError_t err = cudaSetDevice(e->device);
