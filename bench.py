@@ -215,6 +215,21 @@ def cufft_plain_leg(seed, keys, eng, steps):
         cp.close()
 
 
+def max_over_ranks(values, dist, device):
+    """Element-wise maximum of per-rank times (the slowest replica sets the job's time)."""
+    if dist is None:
+        return [float(x) for x in values]
+    import torch
+    t = torch.tensor([float(x) for x in values], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_value(world, steps, bits, seconds):
+    """Whole-job key Gbit/s: every rank processed `steps` blocks of `bits` in at most `seconds`."""
+    return world * steps * bits / seconds / 1e9
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -305,11 +320,8 @@ def run_ours(args):
     stats = eng.sync()
     stage_ms, stage_blocks = eng.stage_times()
     eng.set_timing(False)
-    t_dev = ev0.elapsed_time(ev1) / 1e3
+    t_dev = max_over_ranks([ev0.elapsed_time(ev1) / 1e3], dist, dev)[0]
     if dist:
-        t = torch.tensor([t_dev], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_dev = float(t.item())
         dist.barrier()
 
     # ---------------------------------------------------------------- e2e through the C ABI
@@ -367,10 +379,7 @@ def run_ours(args):
     t_e2e = time.perf_counter() - t0
     same_out = bool((pin_outs[(args.steps - 1) % depth] == eng.process(*keys[(args.steps - 1) % len(keys)],
                                                                        N_BITS, V_BITS)).all())
-    if dist:
-        t = torch.tensor([t_e2e, t_e2e_sync], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e, t_e2e_sync = float(t[0].item()), float(t[1].item())
+    t_e2e, t_e2e_sync = max_over_ranks([t_e2e, t_e2e_sync], dist, dev)
     h2d = (H_BITS // 32 + 1) * 4 + (V_BITS // 32) * 4
     d2h = nbytes_out
 
@@ -412,7 +421,7 @@ def run_ours(args):
         cb, cores, sample = cpu_baseline()
         cpu = {"value": cb, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
 
-    value = world * args.steps * N_BITS / t_dev / 1e9
+    value = job_value(world, args.steps, N_BITS, t_dev)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
@@ -420,10 +429,10 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "n": N_BITS, "h": H_BITS, "v": V_BITS, "blocks_per_step": 1,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2: 512 MiB work array + 512 MiB seed spectrum per block"},
-        "e2e": {"value": world * args.steps * N_BITS / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": job_value(world, args.steps, N_BITS, t_e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "pa_submit/pa_poll, 2 blocks in flight, pinned host buffers",
                 "output_equals_pa_process": same_out,
-                "sync_value": world * args.steps * N_BITS / t_e2e_sync / 1e9,
+                "sync_value": job_value(world, args.steps, N_BITS, t_e2e_sync),
                 "sync_api": "pa_process, one block at a time"},
         "gpu_launches": args.steps * pa.kernels_per_block(N_BITS, V_BITS),
         "kernels_ms": kern, "kernel_blocks_timed": stage_blocks,
