@@ -283,6 +283,7 @@ __global__ void __launch_bounds__(256, 2)
     float2* tws = u2 + CPT * U2N;        // [QB | 2 | QB | QL (unless LEAN)][NT] per-thread stage bases
     constexpr int U1D = U1N > 0 ? U1N : 1, U2D = U2N > 0 ? U2N : 1;  // divisors (unused when LEAN)
     __shared__ __align__(8) uint64_t bar;       // TMA completion of the current tile
+    __shared__ __align__(8) uint64_t bar_spec;  // bulk copy of the tile's seed spectrum (key pass)
     __shared__ int s_fail;                      // a bounded wait expired: stop waiting
     const uint32_t n2 = 1u << g.log_n2;
     const int ntiles = (int)(n2 / CPT);
@@ -354,8 +355,10 @@ __global__ void __launch_bounds__(256, 2)
     if (t == 0) {
         s_fail = 0;
         mbar_init(&bar, 1);
+        mbar_init(&bar_spec, 1);
     }
     __syncthreads();
+    uint32_t parity_spec = 0;
     // The last inverse stage writes straight from registers when the linear map gives each thread both
     // columns of a pair for the same rows; the tile buffer is then free during that stage and the next
     // tile's copies overlap with it.
@@ -414,14 +417,37 @@ __global__ void __launch_bounds__(256, 2)
         } else {
             exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorPair>(x, sm);
         }
+        float2* tspec = spec + (size_t)tile * (CPT * L);
+        const bool special = tile == 0;  // pair 0 holds the self-mirrored columns 0 and N2/2
+        // Key pass: the tile buffer is free until the inverse exchange, so the tile's seed spectrum
+        // (CPT * L values, contiguous) is copied into it while the mirror stage computes, and the
+        // spectral step reads shared memory instead of waiting on L2.
+        const bool spec_smem = !SEED && !special;
+        if (spec_smem) {
+            __syncthreads();  // every thread done reading sm
+            fence_proxy_async();
+            if (t == 0) {
+                constexpr uint32_t kBytes = CPT * L * sizeof(float2), kChunk = 16384;
+                mbar_expect_tx(&bar_spec, kBytes);
+#pragma unroll 1
+                for (uint32_t off = 0; off < kBytes; off += kChunk)
+                    bulk_load(reinterpret_cast<char*>(sm) + off, reinterpret_cast<const char*>(tspec) + off, kChunk,
+                              &bar_spec);
+            }
+        }
         {
             float2 w[2] = {tws[QB * NT + t], tws[(QB + 1) * NT + t]};
             stage<16, LR, -1, E>(x, w);
         }
+        if (spec_smem) {
+            if (!s_fail && !mbar_wait(&bar_spec, parity_spec)) {
+                s_fail = 1;
+                atomicExch(err, kErrTmaTimeout);
+            }
+            parity_spec ^= 1u;
+        }
 
         // ---- spectral step: real split, product with the seed spectrum, real merge
-        float2* tspec = spec + (size_t)tile * (CPT * L);
-        const bool special = tile == 0;  // pair 0 holds the self-mirrored columns 0 and N2/2
         if (special) {
             __syncthreads();
             if (pp == 0) {
@@ -495,10 +521,11 @@ __global__ void __launch_bounds__(256, 2)
             // W_2N^{p + N2 (jj + LR r)} = W_2N^{p + N2 jj} * W_32^r
             const uint32_t p = (uint32_t)tile * (CPT / 2) + (uint32_t)pp;
             const float2 base = expmi_pi(p + n2 * (uint32_t)jj, g.log_n);
-            const float2* sa = tspec + (2 * pp) * 16 * LR + jj;
-            const float2* sb = tspec + (2 * pp + 1) * 16 * LR + jj;
-            float2* da = reinterpret_cast<float2*>(const_cast<float2*>(sa));
-            float2* db = reinterpret_cast<float2*>(const_cast<float2*>(sb));
+            const float2* sbase = spec_smem ? sm : tspec;  // key pass: the copy in shared memory
+            const float2* sa = sbase + (2 * pp) * 16 * LR + jj;
+            const float2* sb = sbase + (2 * pp + 1) * 16 * LR + jj;
+            float2* da = tspec + (2 * pp) * 16 * LR + jj;
+            float2* db = tspec + (2 * pp + 1) * 16 * LR + jj;
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
                 // W_32^r = e^{-i pi r/16} = (cos, -sin)(2 pi r/32), r < 16
@@ -510,7 +537,15 @@ __global__ void __launch_bounds__(256, 2)
                     __stcs(db + (15 - r) * LR, cscale(xb, sc));
                 } else {
                     float2 qa, qb;
-                    real_merge(cmul(xa, __ldcs(sa + r * LR)), cmul(xb, __ldcs(sb + (15 - r) * LR)), w, qa, qb);
+                    float2 fa, fb;
+                    if (spec_smem) {
+                        fa = sa[r * LR];
+                        fb = sb[(15 - r) * LR];
+                    } else {
+                        fa = __ldcs(sa + r * LR);
+                        fb = __ldcs(sb + (15 - r) * LR);
+                    }
+                    real_merge(cmul(xa, fa), cmul(xb, fb), w, qa, qb);
                     x[r] = qa;
                     x[16 + 15 - r] = qb;
                 }
