@@ -49,6 +49,7 @@ struct Plain {
     uint8_t* h_out = nullptr;
     cudaStream_t s = nullptr;
     bool seed_ready = false;
+    double step_ms[8] = {};  // host wall time of each step of the last block (see cp_step_ms)
 };
 
 // One thread per bit, 1024 bits per block; a set bit stores h1 and adds 1 to the counter.
@@ -202,6 +203,13 @@ CP_API int cp_process(void* h, int recalc_seed, int do_xor, int do_compress, dou
     const uint32_t n = p->n, hl = n - p->v;
     const bool seed = recalc_seed || !p->seed_ready;
     const auto t0 = std::chrono::steady_clock::now();
+    auto tprev = t0;
+    auto mark = [&](int i) {  // each step ends in a host sync, so wall time per step is its cost
+        const auto now = std::chrono::steady_clock::now();
+        p->step_ms[i] = std::chrono::duration<double, std::milli>(now - tprev).count();
+        tprev = now;
+    };
+    for (double& x : p->step_ms) x = 0.0;
     cudaStream_t s = p->s;
     if (seed) {
         CP_TRY(cudaMemsetAsync(p->cnt, 0, 2 * sizeof(uint32_t), s));
@@ -210,27 +218,34 @@ CP_API int cp_process(void* h, int recalc_seed, int do_xor, int do_compress, dou
     } else {
         CP_TRY(cudaMemsetAsync(p->cnt + 1, 0, sizeof(uint32_t), s));
     }
+    mark(0);
     const uint32_t key_words = hl / 32u + 1u;
     k_unpack<<<(key_words * 32u + 1023u) / 1024u, 1024, 0, s>>>(p->h_ks, p->di1, p->cnt + 1);
     CP_TRY(cudaStreamSynchronize(s));
+    mark(1);
     k_correction<<<1, 1, 0, s>>>(p->cnt, p->corr, n);
     CP_TRY(cudaStreamSynchronize(s));
+    mark(2);
     CP_FFT(cufftSetStream(p->fwd, s));
     CP_FFT(cufftExecR2C(p->fwd, p->di1, reinterpret_cast<cufftComplex*>(p->do1)));
     CP_TRY(cudaDeviceSynchronize());
+    mark(3);
     if (seed) {
         CP_FFT(cufftExecR2C(p->fwd, p->di2, reinterpret_cast<cufftComplex*>(p->do2)));
         CP_TRY(cudaDeviceSynchronize());
         p->seed_ready = true;
     }
+    mark(4);
     k_zero_dc<<<1, 2, 0, s>>>(p->do1, p->do2);
     CP_TRY(cudaStreamSynchronize(s));
     const uint32_t bins = n / 2u + 1u;
     k_product<<<(bins + 1023u) / 1024u, bins < 1024u ? bins : 1024u, 0, s>>>(p->do1, p->do2, bins);
     CP_TRY(cudaStreamSynchronize(s));
+    mark(5);
     CP_FFT(cufftSetStream(p->inv, s));
     CP_FFT(cufftExecC2R(p->inv, reinterpret_cast<cufftComplex*>(p->do1), p->di2));
     CP_TRY(cudaDeviceSynchronize());
+    mark(6);
     const float norm = (float)n / (2048.0f * kR) / (2048.0f * kR);
     uint32_t* out = reinterpret_cast<uint32_t*>(p->h_out);
     if (do_xor) {
@@ -240,9 +255,16 @@ CP_API int cp_process(void* h, int recalc_seed, int do_xor, int do_compress, dou
         k_pack<false><<<words / 31u + 1u, 1023, 0, s>>>(p->di2, out, nullptr, p->corr, norm);
     }
     CP_TRY(cudaStreamSynchronize(s));
+    mark(7);
     CP_TRY(cudaGetLastError());
     if (wall_ms) *wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return 0;
+}
+
+// Host wall time (ms) of each step of the last cp_process, 8 values: seed unpack, key unpack,
+// correction, R2C key, R2C seed, zero DC + product, C2R, pack to the pinned output.
+CP_API void cp_step_ms(void* h, double* ms) {
+    for (int i = 0; i < 8; ++i) ms[i] = static_cast<Plain*>(h)->step_ms[i];
 }
 
 // After cp_process: largest distance from the nearest integer over the first out_bits outputs.

@@ -48,6 +48,8 @@ class CufftPlain:
         lib.cp_process.restype = ctypes.c_int
         lib.cp_residual.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
         lib.cp_residual.restype = ctypes.c_int
+        lib.cp_step_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+        lib.cp_step_ms.restype = None
         self._lib, self.n, self.v = lib, n, v
         h = vp()
         rc = lib.cp_create(n, v, ctypes.byref(h))
@@ -84,6 +86,14 @@ class CufftPlain:
         if rc != 0:
             raise RuntimeError("cp_process failed: %d" % rc)
         return ms.value
+
+    STEPS = ("unpack_seed", "unpack_key", "correction", "r2c_key", "r2c_seed", "zero_dc_product", "c2r", "pack")
+
+    def step_ms(self) -> dict:
+        """Host wall ms of each step of the last block (every step ends in a host sync)."""
+        ms = (ctypes.c_double * 8)()
+        self._lib.cp_step_ms(self._h, ms)
+        return {k: ms[i] for i, k in enumerate(self.STEPS)}
 
     def output(self, nbytes: int) -> np.ndarray:
         return self.out[:nbytes].copy()

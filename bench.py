@@ -198,7 +198,7 @@ def cufft_plain_leg(seed, keys, eng, steps):
             p50 = times[len(times) // 2]
             p99 = times[min(len(times) - 1, int(round(0.99 * (len(times) - 1))))]
             res[mode] = {"value": N_BITS / (p50 / 1e3) / 1e9, "unit": UNIT, "p50_ms": p50, "p99_ms": p99,
-                         "blocks": len(times)}
+                         "blocks": len(times), "last_block_steps_ms": cp.step_ms()}
         ks, kr = keys[0]
         cp.load(key_start=ks, key_rest=kr)
         cp.process(recalc_seed=False)

@@ -137,3 +137,28 @@ def test_served_static_seeds_and_busy(torch_cuda, engine):
     for r in reqs:
         want = alone(engine, banks.seed_words(r), banks.key_start(r), banks.key_rest(r), r.n, r.v, r.flags)
         assert np.array_equal(res.outputs[r.rid], want), r
+
+
+def test_served_admission_evicts_idle_slots_within_budget(torch_cuda, engine):
+    """A 30 MB budget holds one 2^21-bit slot (26.5 MB) but not it and a 2^20-bit one: growing blocks
+    make the pool free idle slots first; a block that can never fit is refused with PA_ERR_TOO_LARGE."""
+    engine.set_pool(hbm_budget_bytes=30 << 20, max_slots=4)
+    sizes = [1 << 19, 1 << 20, 1 << 21, 1 << 19, 1 << 21]
+    reqs = []
+    for i, n in enumerate(sizes):
+        v = n // 4 + n // 8
+        reqs.append(W.Request(rid=i, arrival=0.0, n=n, v=v, static=False, seed_word0=64 * i, key_word0=128 * i))
+    words = max(r.n // 32 + max(r.seed_word0, r.key_word0) for r in reqs) + 64
+    banks = W.HostBanks(words)
+    res = W.serve(engine, reqs, banks, out_slots=1, keep=lambda r: True)  # one at a time
+    for r in reqs:
+        want = alone(engine, banks.seed_words(r), banks.key_start(r), banks.key_rest(r), r.n, r.v, r.flags)
+        assert np.array_equal(res.outputs[r.rid], want), r
+    big = W.Request(rid=9, arrival=0.0, n=1 << 22, v=(1 << 20) + (1 << 19), static=False, seed_word0=0, key_word0=0)
+    banks2 = W.HostBanks(big.n // 32 + 64)
+    out = np.zeros(big.v // 8, np.uint8)
+    job = pa.PAJob(banks2.seed_words(big).ctypes.data, -1, banks2.key_start(big).ctypes.data,
+                   banks2.key_rest(big).ctypes.data, big.n, big.v, DEFAULT, out.ctypes.data)
+    with pytest.raises(pa.PAError) as ei:
+        engine.submit(job)
+    assert ei.value.code == pa.PA_ERR_TOO_LARGE
