@@ -502,8 +502,9 @@ def run_dynamic27(args):
     eng.close()
 
 
-def run_exact29(args):
-    """n = 2^29 (beyond the FP32 path): exact NTT path, fresh seed per block."""
+def run_big29(args, force_exact):
+    """n = 2^29 (beyond one FP32 pass), fresh seed per block: 2^27-bit FP32 chunk blocks under the
+    residual guard, or (force_exact) the exact NTT path."""
     import numpy as np
     import torch
     import privacyamplification_gb300 as pa
@@ -522,7 +523,8 @@ def run_exact29(args):
 
     def block(i):
         eng.set_seed_device(seeds[i % 2].data_ptr(), n, 1, stream=stream.cuda_stream)
-        eng.process_device(ks.data_ptr(), kr.data_ptr(), n, v, d_out.data_ptr(), stream=stream.cuda_stream)
+        eng.process_device(ks.data_ptr(), kr.data_ptr(), n, v, d_out.data_ptr(),
+                           flags=pa.DEFAULT_FLAGS | (pa.FLAG_EXACT if force_exact else 0), stream=stream.cuda_stream)
 
     for i in range(args.warmup):
         block(i)
@@ -536,9 +538,11 @@ def run_exact29(args):
         ev1.synchronize()
     st = eng.sync(check=False)
     t = ev0.elapsed_time(ev1) / 1e3
+    path = "exact NTT path mod 3*2^30+1" if force_exact else "FP32 path in 2^27-bit chunk blocks, residual guard"
     _line(METRIC, args.steps * n / t / 1e9, UNIT, args.steps, args.warmup, t / args.steps * 1e3,
-          "n=2^29 (h=n/2+n/8, v=n/4+n/8), dynamic seed, exact NTT path mod 3*2^30+1",
-          {"exact": st.exact, "clocks": clk.summary(), "dtype": "u32 (mod p)"})
+          "n=2^29 (h=n/2+n/8, v=n/4+n/8), dynamic seed, " + path,
+          {"exact": st.exact, "max_residual": st.max_residual, "clocks": clk.summary(),
+           "dtype": "u32 (mod p)" if force_exact else "f32"})
     eng.close()
 
 
@@ -638,7 +642,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT pipeline baseline leg")
     ap.add_argument("--workload", default="static27",
-                    choices=["static27", "dynamic27", "exact29", "batch", "serve", "serve-static"],
+                    choices=["static27", "dynamic27", "dynamic29", "exact29", "batch", "serve", "serve-static"],
                     help="static27 (default): the headline line; the others print their own line")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -647,8 +651,8 @@ def main():
         return run_reference(args)
     if args.workload == "dynamic27":
         return run_dynamic27(args)
-    if args.workload == "exact29":
-        return run_exact29(args)
+    if args.workload in ("dynamic29", "exact29"):
+        return run_big29(args, force_exact=args.workload == "exact29")
     if args.workload == "batch":
         return run_batch(args)
     if args.workload in ("serve", "serve-static"):

@@ -19,7 +19,8 @@
  *   - Result: out[i] = (sum_{j=0..h} key_start[j] * seed[(i-j) mod n] mod 2) XOR key_rest[i].
  *   - Precision: the FP32 FFT path measures every block's largest distance of an output value to the
  *     nearest integer; above residual_limit pa_process recomputes the block on the exact integer
- *     (NTT mod 3*2^30+1) path, which also serves every n > 2^27 (up to 2^30).
+ *     (NTT mod 3*2^30+1) path.  Blocks with n > 2^27 (up to 2^30) run as 2^27-bit FP32 chunk blocks
+ *     (large-block decomposition) under the same guard.
  *
  * All functions return 0 (PA_OK) or a negative PA_ERR_* code; nothing exits the process.
  * An engine is bound to one CUDA device and must be used from one host thread at a time.
@@ -69,8 +70,8 @@ typedef struct pa_stats {
     uint64_t popcount_seed;   /* Hamming weight of the seed (count_one_of_global_seed) */
     float gpu_ms;             /* device time of the block (CUDA events) */
     int32_t seed_uses_left;   /* remaining blocks for the cached seed, -1 = unlimited */
-    int32_t exact;            /* 1: the output came from the exact path (guard fallback, PA_FLAG_EXACT or
-                                 n > 2^27), 0: from the FP32 path */
+    int32_t exact;            /* 0: FP32 path, one pass; 2: FP32 path as 2^27-bit chunk blocks (n > 2^27);
+                                 1: exact path (guard fallback or PA_FLAG_EXACT).  Popcounts are 0 for 1, 2 */
 } pa_stats;
 
 /* Creates an engine on cfg->device_id and allocates its HBM working set for n <= max_sample_size.

@@ -1,0 +1,135 @@
+// pa_chunk.cu -- blocks beyond the single-pass FP32 size (n > 2^27) as 2^27-bit FP32 chunk blocks.
+//
+// The block's result bit i (i < out_bits) is XOR_{j <= h} key_start[j] AND T[i - j] with
+// T[m] = seed[m mod n], a linear Toeplitz product.  Rows i and key positions j are cut into chunks of
+// side s = 2^26; chunk (a, b) is one key block of n' = 2s, v' = h' = s (no XOR, no compression) with
+// key_start' = key_start[b s .. b s + s) followed by a zero bit and seed' = T[d s, d s + s) followed by
+// T[d s - s, d s) for d = a - b -- the technique of the reference's examples/LargeBlocksizeExample
+// (GetLocalSeed / GetLocalKey / XorWithRow, main.cpp:104-124), run on the device.  Chunks on one
+// diagonal d share seed' and so one seed spectrum.  The kernels here move the chunk inputs and
+// combine the chunk outputs; the chunk blocks themselves are the ordinary three-pass kernels.
+#include "pa_kernels.cuh"
+
+namespace pa {
+
+namespace {
+
+constexpr uint32_t kXorFlag = 1u;  // PA_FLAG_XOR_KEY_REST
+
+// dst[i] = seed[(start + i) mod nw], i < count (whole 32-bit words; start may be negative).
+__global__ void k_seed_window(uint32_t* __restrict__ dst, const uint32_t* __restrict__ seed, uint32_t nw,
+                              long long start, uint32_t count) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        long long src = (start + (long long)i) % (long long)nw;
+        if (src < 0) src += nw;
+        dst[i] = __ldg(seed + src);
+    }
+}
+
+// Key chunk: sw words of key_start from bit `first` (a multiple of 32), bits past h cleared, then one
+// zero word (its first bit is the chunk's bit h' = s).
+__global__ void k_key_chunk(uint32_t* __restrict__ dst, const uint32_t* __restrict__ ks, unsigned long long first,
+                            uint32_t sw, uint32_t h) {
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w <= sw; w += gridDim.x * blockDim.x) {
+        const unsigned long long bit = first + 32ull * w;
+        uint32_t v = 0u;
+        if (w < sw && bit <= h) {
+            v = __ldg(ks + (bit >> 5));
+            if (bit + 31 > h) v &= ~(0xFFFFFFFFu >> (uint32_t)(h - bit + 1));
+        }
+        dst[w] = v;
+    }
+}
+
+__global__ void k_xor_rows(uint32_t* __restrict__ acc, const uint32_t* __restrict__ add, uint32_t words) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < words; i += gridDim.x * blockDim.x) acc[i] ^= add[i];
+}
+
+// Output words (reference byte-stream order) = accumulated rows XOR key_rest (byte-swapped words).
+__global__ void k_chunk_final(uint32_t* __restrict__ out, const uint32_t* __restrict__ acc,
+                              const uint32_t* __restrict__ key_rest, uint32_t words, uint32_t v, uint32_t flags) {
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x) {
+        uint32_t x = acc[w];
+        if ((flags & kXorFlag) && 32ull * w < v) x ^= __byte_perm(__ldg(key_rest + w), 0, 0x0123);
+        out[w] = x;
+    }
+}
+
+__global__ void k_max_words(unsigned int* __restrict__ dst, const unsigned int* __restrict__ src, int count) {
+    unsigned int m = 0u;
+    for (int i = threadIdx.x; i < count; i += blockDim.x) m = max(m, src[i]);
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(dst, m);
+}
+
+int grid_for(uint32_t items, int num_sms) {
+    uint32_t b = (items + 255u) / 256u;
+    const uint32_t cap = 4u * (uint32_t)num_sms;
+    return (int)(b < 1u ? 1u : (b > cap ? cap : b));
+}
+
+}  // namespace
+
+ChunkPlan chunk_plan(const BlockGeom& g) {
+    ChunkPlan p;
+    p.side = 1u << kChunkLog;
+    p.rows = (g.out_bits + p.side - 1u) / p.side;
+    p.cols = (uint32_t)(((uint64_t)g.h + 1u + p.side - 1u) / p.side);
+    p.chunks = p.rows * p.cols;
+    p.diagonals = p.rows + p.cols - 1u;
+    return p;
+}
+
+size_t chunk_staging_words(const BlockGeom& g) {
+    const ChunkPlan p = chunk_plan(g);
+    const size_t sw = p.side / 32u;
+    return 5 * sw + (size_t)p.rows * sw + p.chunks + 64;
+}
+
+int chunk_kernel_count(const BlockGeom& g, const BlockGeom& gc) {
+    const ChunkPlan p = chunk_plan(g);
+    // per diagonal: 2 window copies + seed spectrum (3); per chunk: key chunk, key block, xor; then 2
+    return (int)(p.diagonals * 5u + p.chunks * (2u + (uint32_t)kernel_count_key_block(gc)) + 2u);
+}
+
+int launch_chunked_block(const BlockGeom& g, const BlockGeom& gc, const uint32_t* seed, const uint32_t* key_start,
+                         const uint32_t* key_rest, uint32_t flags, uint32_t* out_words, uint32_t* staging,
+                         float2* spec, const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits,
+                         int num_sms, cudaStream_t s) {
+    const ChunkPlan p = chunk_plan(g);
+    const uint32_t sw = p.side / 32u, nw = g.n / 32u;
+    uint32_t* seedwin = staging;            // 2 sw words
+    uint32_t* keyc = staging + 2 * sw;      // sw + 1 words (2 sw reserved)
+    uint32_t* cout = staging + 4 * sw;      // sw words
+    uint32_t* acc = staging + 5 * sw;       // rows * sw words
+    unsigned int* res = reinterpret_cast<unsigned int*>(acc + (size_t)p.rows * sw);  // one per chunk
+    cudaError_t err = cudaMemsetAsync(acc, 0, (size_t)p.rows * sw * sizeof(uint32_t), s);
+    if (err != cudaSuccess) return (int)err;
+    const int gw = grid_for(sw, num_sms);
+    uint32_t idx = 0;
+    for (int d = -(int)(p.cols - 1); d < (int)p.rows; ++d) {
+        const int a0 = d > 0 ? d : 0;
+        const int a1 = (int)p.rows < (int)p.cols + d ? (int)p.rows : (int)p.cols + d;
+        if (a0 >= a1) continue;
+        k_seed_window<<<gw, 256, 0, s>>>(seedwin, seed, nw, (long long)d * sw, sw);
+        k_seed_window<<<gw, 256, 0, s>>>(seedwin + sw, seed, nw, (long long)(d - 1) * sw, sw);
+        int rc = launch_seed_spectrum(gc, seedwin, spec, sc, cnt + 1, num_sms, s);
+        if (rc) return rc;
+        for (int a = a0; a < a1; ++a) {
+            const int b = a - d;
+            k_key_chunk<<<gw, 256, 0, s>>>(keyc, key_start, (unsigned long long)b * p.side, sw, g.h);
+            rc = launch_key_block(gc, keyc, nullptr, 0u, spec, sc, cnt, res + idx, cout, num_sms, s, nullptr);
+            if (rc) return rc;
+            k_xor_rows<<<gw, 256, 0, s>>>(acc + (size_t)a * sw, cout, sw);
+            ++idx;
+        }
+    }
+    err = cudaMemsetAsync(resid_bits, 0, sizeof(unsigned int), s);
+    if (err != cudaSuccess) return (int)err;
+    k_max_words<<<1, 256, 0, s>>>(resid_bits, res, (int)idx);
+    const uint32_t owords = (g.out_bits + 31u) / 32u;
+    k_chunk_final<<<grid_for(owords, num_sms), 256, 0, s>>>(out_words, acc, key_rest, owords, g.v, flags);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace pa

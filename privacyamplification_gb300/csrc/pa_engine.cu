@@ -106,8 +106,29 @@ int seed_common(pa_engine* e, uint32_t n, int32_t reuse, cudaStream_t s) {
         BlockGeom g;
         int rc = make_geom(n, n / 2u, PA_FLAG_COMPRESS, e->split, &g);
         if (rc) return rc;
+        if (g.exact_only) return PA_OK;  // chunk spectra are built per block, the exact transform on demand
         return build_spectrum(e, g, s);
     }
+    return PA_OK;
+}
+
+// n > 2^27: the block as 2^27-bit FP32 chunk blocks (pa_chunk.cu).  The exact seed transform's buffer
+// is the chunks' staging area and the chunk spectra go through d_spec, so both caches are invalidated.
+// Block popcounts are not formed on this path (read_stats reports 0).
+int chunked_block(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const BlockGeom& g, uint32_t flags,
+                  uint32_t* d_out, cudaStream_t s) {
+    BlockGeom gc;
+    const uint32_t side = 1u << pa::kChunkLog;
+    int rc = make_geom(2u * side, side, 0u, e->split, &gc);
+    if (rc) return rc;
+    if (pa::chunk_staging_words(g) > (size_t(1) << e->cap_log_np)) return PA_ERR_TOO_LARGE;
+    rc = ensure_maps(e, gc);
+    if (rc) return rc;
+    e->exact_valid = false;
+    e->spec_valid = false;
+    rc = pa::launch_chunked_block(g, gc, e->d_seed, d_ks, d_kr, flags, d_out, e->d_exact_seed, e->d_spec, scratch(e),
+                                  e->d_cnt, e->d_resid, e->num_sms, s);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
     return PA_OK;
 }
 
@@ -130,7 +151,8 @@ int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const
                  uint32_t* d_out, cudaStream_t s) {
     if (!e->seed_valid || e->seed_left == 0) return PA_ERR_NO_SEED;
     if (g.n != e->seed_n) return PA_ERR_INVALID_ARG;
-    if (g.exact_only || (flags & PA_FLAG_EXACT)) {
+    e->last_chunked = false;
+    if (flags & PA_FLAG_EXACT) {
         PA_CUDA(e, cudaEventRecord(e->ev0, s));
         int rc = exact_block(e, d_ks, d_kr, g, flags, d_out, s);
         if (rc) return rc;
@@ -140,6 +162,15 @@ int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const
         return PA_OK;
     }
     e->last_exact = false;
+    if (g.exact_only) {
+        PA_CUDA(e, cudaEventRecord(e->ev0, s));
+        int rc = chunked_block(e, d_ks, d_kr, g, flags, d_out, s);
+        if (rc) return rc;
+        PA_CUDA(e, cudaEventRecord(e->ev1, s));
+        e->last_chunked = true;
+        if (e->seed_left > 0) --e->seed_left;
+        return PA_OK;
+    }
     if (!e->spec_valid || !same_seed_geom(e->spec_geom, g)) {
         int rc = build_spectrum(e, g, s);
         if (rc) return rc;
@@ -180,13 +211,14 @@ int read_stats(pa_engine* e, pa_stats* st, float* resid_out) {
     *resid_out = resid;
     if (st) {
         st->max_residual = resid;
-        st->popcount_key = cnt[0];
-        st->popcount_seed = cnt[1];
+        const bool counted = !e->last_exact && !e->last_chunked;  // popcounts exist on the one-pass FP32 path
+        st->popcount_key = counted ? cnt[0] : 0;
+        st->popcount_seed = counted ? cnt[1] : 0;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e->ev0, e->ev1);
         st->gpu_ms = ms;
         st->seed_uses_left = e->seed_left < 0 ? -1 : (int32_t)e->seed_left;
-        st->exact = e->last_exact ? 1 : 0;
+        st->exact = e->last_exact ? 1 : (e->last_chunked ? 2 : 0);
     }
     return PA_OK;
 }
@@ -202,7 +234,12 @@ size_t pa_output_bytes(uint32_t n, uint32_t v, uint32_t flags) {
 int pa_kernels_per_block(uint32_t n, uint32_t v, uint32_t flags) {
     BlockGeom g;
     if (make_geom(n, v, flags, nullptr, &g)) return 0;
-    if (g.exact_only || (flags & PA_FLAG_EXACT)) return pa::exact_kernel_count(g);
+    if (flags & PA_FLAG_EXACT) return pa::exact_kernel_count(g);
+    if (g.exact_only) {
+        BlockGeom gc;
+        if (make_geom(2u << pa::kChunkLog, 1u << pa::kChunkLog, 0u, nullptr, &gc)) return 0;
+        return pa::chunk_kernel_count(g, gc);
+    }
     return pa::kernel_count_key_block(g);
 }
 

@@ -36,6 +36,7 @@ struct pa_engine {
     pa::NttTables* ntt = nullptr;      // exact-path twiddle tables
     bool exact_valid = false;          // d_exact_seed matches the current seed for exact_geom
     bool last_exact = false;           // the last block ran on the exact path
+    bool last_chunked = false;         // the last block ran as FP32 chunk blocks (n > 2^27)
     pa::BlockGeom exact_geom{};
     pa::PassMaps maps{};        // tensor maps for the geometry maps_key
     int maps_key = -1;

@@ -85,4 +85,20 @@ int launch_exact_block(const BlockGeom& g, const uint32_t* key_start, const uint
                        const uint32_t* seed_hat, uint32_t* a, uint32_t* tmp, uint32_t* out_words, NttTables** tables,
                        cudaStream_t s);
 int exact_kernel_count(const BlockGeom& g);
+
+// Blocks beyond the single-pass FP32 size (pa_chunk.cu): side x side chunk blocks (n' = 2 side) on the
+// FP32 path.  gc: geometry of a chunk block (n' = 2 side, v' = side, no flags).  staging:
+// chunk_staging_words(g) words; spec / sc / cnt: the FP32 path's buffers for gc.  resid_bits receives
+// the largest chunk residual.
+constexpr int kChunkLog = 26;
+struct ChunkPlan {
+    uint32_t side, rows, cols, chunks, diagonals;
+};
+ChunkPlan chunk_plan(const BlockGeom& g);
+size_t chunk_staging_words(const BlockGeom& g);
+int chunk_kernel_count(const BlockGeom& g, const BlockGeom& gc);
+int launch_chunked_block(const BlockGeom& g, const BlockGeom& gc, const uint32_t* seed, const uint32_t* key_start,
+                         const uint32_t* key_rest, uint32_t flags, uint32_t* out_words, uint32_t* staging,
+                         float2* spec, const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits,
+                         int num_sms, cudaStream_t s);
 }  // namespace pa

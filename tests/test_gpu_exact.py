@@ -89,8 +89,9 @@ def big_engine(pa_lib):
 
 
 def test_config3_2p29_dynamic_seed(big_engine):
-    """n = 2^29, h = n/2+n/8, v = n/4+n/8, a fresh seed per block: sampled rows against the direct
-    oracle, GF(2) linearity in the key for a fixed seed, and the key_rest XOR."""
+    """n = 2^29, h = n/2+n/8, v = n/4+n/8, a fresh seed per block (FP32 path in 2^27-bit chunk blocks):
+    sampled rows against the direct oracle, GF(2) linearity in the key for a fixed seed, and the
+    key_rest XOR."""
     n, v = std_sizes(1 << 29)
     rng = np.random.default_rng(29)
     outs = []
@@ -99,7 +100,7 @@ def test_config3_2p29_dynamic_seed(big_engine):
         ks, kr = O.key_split(recv, n, v)
         big_engine.set_seed(seed, n, 0)
         out = big_engine.process(ks, kr, n, v)
-        assert big_engine.last_stats.exact == 1
+        assert big_engine.last_stats.exact == 2 and big_engine.last_stats.max_residual < 0.1
         blk = O.DirectBlock(seed, ks, n, v)
         krb = O.bits_msb(kr, v).astype(np.uint8)
         for r0 in [0, v - 64] + [int(x) * 64 for x in rng.integers(0, v // 64, 3)]:
@@ -115,3 +116,36 @@ def test_config3_2p29_dynamic_seed(big_engine):
     assert np.array_equal(o12, o1 ^ o2)
     ox = big_engine.process(ks1, kr1, n, v, DEFAULT)
     assert np.array_equal(ox, o1 ^ kr1.astype(">u4").view(np.uint8))
+
+
+@pytest.mark.parametrize("n,v,flags", [(1 << 28, (1 << 26) + (1 << 25), DEFAULT),
+                                       ((1 << 28) + (1 << 20), 100663296, pa.FLAG_COMPRESS),
+                                       ((1 << 28) - 1024, 33554432, pa.FLAG_XOR_KEY_REST)])
+def test_chunked_fp32_equals_exact_path(big_engine, n, v, flags):
+    """Blocks beyond 2^27 bits: the FP32 chunk path reproduces the exact path bit for bit (whole
+    output), powers of two and not, with and without compression / XOR."""
+    seed, recv = O.random_block(n, v, n % 1000 + flags)
+    ks, kr = pa.key_split(recv, n, v)
+    big_engine.set_seed(seed, n, -1)
+    out = big_engine.process(ks, kr, n, v, flags)
+    assert big_engine.last_stats.exact == 2 and big_engine.last_stats.max_residual < 0.1
+    ref = big_engine.process(ks, kr, n, v, flags | pa.FLAG_EXACT)
+    assert big_engine.last_stats.exact == 1
+    assert np.array_equal(out, ref)
+
+
+def test_chunked_guard_falls_back_to_exact(big_engine):
+    """Run-structured block at n = 2^28: the chunk residuals exceed the budget and the block is
+    recomputed on the exact path."""
+    n, v = std_sizes(1 << 28)
+    seed, recv = run_structured(n, v)
+    ks, kr = pa.key_split(recv, n, v)
+    big_engine.set_seed(seed, n, -1)
+    out = big_engine.process(ks, kr, n, v)
+    st = big_engine.last_stats
+    assert st.max_residual > 0.25 and st.exact == 1
+    blk = O.DirectBlock(seed, ks, n, v)
+    krb = O.bits_msb(kr, v).astype(np.uint8)
+    for r0 in (0, v // 2 // 64 * 64, v - 64):
+        assert np.array_equal(np.unpackbits(out[r0 // 8: r0 // 8 + 8]), blk.rows(r0, r0 + 64) ^ krb[r0: r0 + 64])
+    blk.close()

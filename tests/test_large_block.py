@@ -78,7 +78,8 @@ def test_decomposition_on_gpu_matches_single_block(gpu_engine, golden):
 
 @pytest.mark.gpu
 def test_decomposition_2p28_fp32_chunks_equal_exact_block(pa_lib):
-    """n = 2^28 is beyond the FP32 single-block path: 2^27-bit FP32 chunks reproduce the exact block."""
+    """n = 2^28 is beyond one FP32 pass: the Python decomposition with 2^27-bit chunk blocks and the
+    engine's own chunked block both reproduce the exact path."""
     n = 1 << 28
     v = n // 4 + n // 8
     rng = np.random.default_rng(28)
@@ -87,7 +88,9 @@ def test_decomposition_2p28_fp32_chunks_equal_exact_block(pa_lib):
     ks, kr = pa.key_split(recv, n, v)
     with pa.Engine(max_sample_size=n) as eng:
         eng.set_seed(seed, n, -1)
-        want = eng.process(ks, kr, n, v)
+        want = eng.process(ks, kr, n, v, DEFAULT | pa.FLAG_EXACT)
         assert eng.last_stats.exact == 1
+        chunked = eng.process(ks, kr, n, v)
+        assert eng.last_stats.exact == 2
         got = L.hash_large_block(eng, seed, ks, kr, n, v, side=1 << 26)
-    assert np.array_equal(got, want)
+    assert np.array_equal(got, want) and np.array_equal(chunked, want)
