@@ -215,6 +215,13 @@ def cufft_plain_leg(seed, keys, eng, steps):
         cp.close()
 
 
+def pct(xs, q):
+    """Nearest-rank percentile."""
+    import math
+    ys = sorted(xs)
+    return ys[min(len(ys) - 1, max(0, math.ceil(q / 100.0 * len(ys)) - 1))]
+
+
 def max_over_ranks(values, dist, device):
     """Element-wise maximum of per-rank times (the slowest replica sets the job's time)."""
     if dist is None:
@@ -306,11 +313,14 @@ def run_ours(args):
     torch.cuda.synchronize()
     eng.set_timing(True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # one event after every block as well (recording an event adds no work): per-block device times
+    ev_blk = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(local) as clk:
         with torch.cuda.stream(stream):
             ev0.record(stream)
             for i in range(args.steps):
                 block(i)
+                ev_blk[i].record(stream)
             ev1.record(stream)
         ev1.synchronize()
         # keep the sampler alive for a short tail so that very short runs still get a sample
@@ -321,6 +331,7 @@ def run_ours(args):
     stage_ms, stage_blocks = eng.stage_times()
     eng.set_timing(False)
     t_dev = max_over_ranks([ev0.elapsed_time(ev1) / 1e3], dist, dev)[0]
+    blk_ms = [ev0.elapsed_time(ev_blk[0])] + [ev_blk[i - 1].elapsed_time(ev_blk[i]) for i in range(1, args.steps)]
     if dist:
         dist.barrier()
 
@@ -338,9 +349,12 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    sync_ms = []
     for i in range(args.steps):
         ks, kr = pin_keys[i % len(pin_keys)]
+        t1 = time.perf_counter()
         eng.process(ks, kr, N_BITS, V_BITS, out=pin_out)
+        sync_ms.append((time.perf_counter() - t1) * 1e3)
     t_e2e_sync = time.perf_counter() - t0
 
     # pipelined form of the same calls: pa_submit / pa_poll with two blocks in flight, so one block's
@@ -435,6 +449,10 @@ def run_ours(args):
                 "sync_value": job_value(world, args.steps, N_BITS, t_e2e_sync),
                 "sync_api": "pa_process, one block at a time"},
         "gpu_launches": args.steps * pa.kernels_per_block(N_BITS, V_BITS),
+        "latency_ms": {"device_p50": pct(blk_ms, 50), "device_p99": pct(blk_ms, 99), "device_max": max(blk_ms),
+                       "pa_process_p50": pct(sync_ms, 50), "pa_process_p99": pct(sync_ms, 99),
+                       "what": "device: CUDA events between consecutive blocks on the engine stream; "
+                               "pa_process: host wall time of one synchronous call (copies in, block, copy out)"},
         "kernels_ms": kern, "kernel_blocks_timed": stage_blocks,
         "block_hbm_model": {"bytes": block_bytes, "GB_per_s_at_kernel_sum": block_bytes / total_s / 1e9
                             if total_s else None},
