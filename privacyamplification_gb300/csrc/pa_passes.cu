@@ -75,6 +75,10 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Waits until at most N of this thread's committed copy groups are still in flight.
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 __device__ __forceinline__ uint32_t load_bit(const uint32_t* __restrict__ w, uint64_t x) {
     return (__ldg(w + (x >> 5)) >> (31u - (uint32_t)(x & 31u))) & 1u;
@@ -143,7 +147,7 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     extern __shared__ float2 sm[];
     __shared__ float2 rho[16], t1[T1N], t2[T2N];
     __shared__ float2 tws[(QB > 0 ? QB : 1) + 2][NT];
-    __shared__ uint32_t bits[L / 16];
+    __shared__ __align__(16) uint32_t bits[2][L / 16];  // double buffer: this row, next row
     __shared__ unsigned long long red[32];
     const uint32_t n1 = 1u << g.log_n1;
     const int t = threadIdx.x;
@@ -161,15 +165,18 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     tws[QB][t] = wm[0];
     tws[QB + 1][t] = wm[1];
     uint32_t ones = 0;
-    for (uint32_t m1 = blockIdx.x; m1 < n1; m1 += gridDim.x) {
-        __syncthreads();  // previous row done with bits / tables / sm
-        const uint32_t* rw = rows + (size_t)m1 * (L / 16);
-#pragma unroll
-        for (int i = 0; i < L / 16 / NT; ++i) {
-            uint32_t w = __ldg(rw + t + i * NT);
-            bits[t + i * NT] = w;
-            ones += __popc(w);
-        }
+    // A row's bits (L/16 words, two per thread) are copied asynchronously one row ahead.
+    static_assert(L / 16 == 2 * NT, "two bit words per thread");
+    auto fetch_row = [&](uint32_t r, int buf) {
+        if (r < n1) cp_async8(&bits[buf][2 * t], rows + (size_t)r * (L / 16) + 2 * t);
+        cp_async_commit();
+    };
+    fetch_row(blockIdx.x, 0);
+    int buf = 0;
+    for (uint32_t m1 = blockIdx.x; m1 < n1; m1 += gridDim.x, buf ^= 1) {
+        __syncthreads();  // previous row done with bits[buf ^ 1] / tables / sm
+        fetch_row(m1 + gridDim.x, buf ^ 1);
+        cp_async_wait_group<1>();  // this thread's copy of row m1 has landed
         for (int i = t; i < 16 + T1N + T2N; i += NT) {  // W_N^{m1 LR r}, W_N^{m1 i}, W_N^{m1 T1N i}
             uint64_t e = i < 16 ? (uint64_t)LR * (uint64_t)i : (i < 16 + T1N ? (uint64_t)(i - 16)
                                                                                 : (uint64_t)T1N * (uint64_t)(i - 16 - T1N));
@@ -178,7 +185,8 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
             else if (i < 16 + T1N) t1[i - 16] = w;
             else t2[i - 16 - T1N] = w;
         }
-        __syncthreads();
+        __syncthreads();  // all copies of row m1 and the tables visible
+        ones += __popc(bits[buf][2 * t]) + __popc(bits[buf][2 * t + 1]);
         float2 x[E];
 #pragma unroll
         for (int q = 0; q < E / P::RA; ++q) {
@@ -186,7 +194,7 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
 #pragma unroll
             for (int r = 0; r < P::RA; ++r) {
                 const int m2 = j + r * (L / P::RA);
-                const uint32_t w = bits[m2 >> 4];
+                const uint32_t w = bits[buf][m2 >> 4];
                 const int sh = 30 - 2 * (m2 & 15);
                 x[q * P::RA + r] = make_float2((float)((w >> (sh + 1)) & 1u), (float)((w >> sh) & 1u));
             }
