@@ -608,6 +608,7 @@ def run_serve(args, static):
     from privacyamplification_gb300 import workloads as W
     pa.load_library()
     eng = pa.Engine(max_sample_size=1 << 27)
+    reserved = eng.pool_reserve(1 << 27, 16)  # every slot's working set exists before the first request
     rates = [(10, 100), (100, 400), (500, 1000), (2000, 2000)]
     all_reqs = {rate: W.poisson_requests(rate, count, static=static, rng_seed=rate) for rate, count in rates}
     words = max(r.n // 32 + max(r.seed_word0, r.key_word0) for rs in all_reqs.values() for r in rs) + 64
@@ -647,7 +648,8 @@ def run_serve(args, static):
           + ("rounded to a power of two, static seed spectra cached per size" if static
              else "(multiple of 1024), each request with its own seed")
           + ", v/n ~ U[0.2,0.8]; continuous admission to slots",
-          {"rates": lines, "mix_equals_alone": {"checked": checked, "mismatched": mismatched}}, higher=False)
+          {"rates": lines, "mix_equals_alone": {"checked": checked, "mismatched": mismatched},
+           "slots_reserved": reserved}, higher=False)
     eng.close()
 
 

@@ -145,6 +145,12 @@ typedef struct pa_job {
  * of slots (0 = 16) and the slots one batch spreads over (0 = 8).  Idle slots are freed first. */
 PA_API int pa_set_pool(pa_engine* e, uint64_t hbm_budget_bytes, int32_t max_slots, int32_t batch_slots);
 
+/* Creates idle slots up front so that later admissions (pa_submit) and batches find their working set
+ * ready instead of allocating it: up to `count` slots (within max_slots and the HBM budget) that hold
+ * blocks with cyclic length up to max_np (a power of two; n itself for power-of-two n).  Returns the
+ * number of slots that now hold such blocks, or a negative PA_ERR_* code. */
+PA_API int pa_pool_reserve(pa_engine* e, uint32_t max_np, int32_t count);
+
 /* Static seeds: computes and keeps the FP32 spectrum of a seed (host words, n/32) for blocks of
  * geometry (n, v, flags) -- for a power-of-two n any v and flags share it.  Synchronous.  The id is
  * valid until pa_seed_cache_clear.  Replaces the reference's reuse of do2 across blocks

@@ -41,7 +41,7 @@ EXPORTS = ("pa_create", "pa_destroy", "pa_set_seed", "pa_process", "pa_set_seed_
            "pa_sync", "pa_key_split", "pa_output_bytes", "pa_kernels_per_block", "pa_set_timing",
            "pa_stage_times", "pa_error_string", "pa_last_cuda_error", "pa_process_noalloc", "pa_set_pool",
            "pa_seed_cache_add", "pa_seed_cache_clear", "pa_batch_run", "pa_batch_sync", "pa_submit", "pa_poll",
-           "pa_set_split", "pa_get_split", "pa_autotune")
+           "pa_set_split", "pa_get_split", "pa_autotune", "pa_pool_reserve")
 
 
 class PAError(RuntimeError):
@@ -119,6 +119,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pa_set_split": ([eng, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
         "pa_get_split": ([eng, ctypes.c_uint32], ctypes.c_int),
         "pa_autotune": ([eng, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+        "pa_pool_reserve": ([eng, ctypes.c_uint32, ctypes.c_int32], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -257,6 +258,13 @@ class Engine:
     # ---- batched and served blocks (slot pool) ------------------------------------------------------
     def set_pool(self, hbm_budget_bytes: int = 0, max_slots: int = 0, batch_slots: int = 0):
         self._check(self._lib.pa_set_pool(self._h, hbm_budget_bytes, max_slots, batch_slots), "pa_set_pool")
+
+    def pool_reserve(self, max_np: int, count: int) -> int:
+        """Creates idle slots for cyclic length <= max_np up front; returns how many such slots exist."""
+        rc = self._lib.pa_pool_reserve(self._h, max_np, count)
+        if rc < 0:
+            self._check(rc, "pa_pool_reserve")
+        return rc
 
     def seed_cache_add(self, seed_words, n: int, v: int, flags: int = DEFAULT_FLAGS) -> int:
         s = _u32(seed_words)

@@ -338,6 +338,28 @@ int pa_set_pool(pa_engine* e, uint64_t hbm_budget_bytes, int32_t max_slots, int3
     return PA_OK;
 }
 
+int pa_pool_reserve(pa_engine* e, uint32_t max_np, int32_t count) {
+    if (!e || count < 0 || max_np < 1024u || (max_np & (max_np - 1u))) return PA_ERR_INVALID_ARG;
+    const int cap = ceil_log2(max_np);
+    if (cap > kFp32MaxLogNp) return PA_ERR_TOO_LARGE;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    Pool* p = get_pool(e);
+    if (!p) return PA_ERR_CUDA;
+    int have = 0;
+    for (Slot* c : p->slots) have += c->cap >= cap ? 1 : 0;
+    while (have < count && (int)p->slots.size() < p->max_slots) {
+        if (p->used + slot_bytes(cap) > p->budget) break;
+        Slot* sl = nullptr;
+        int rc = new_slot(e, p, cap, &sl);
+        if (rc) return rc;
+        sl->last_use = ++p->clock;
+        p->slots.push_back(sl);
+        ++have;
+    }
+    drop_graphs(p);
+    return have;
+}
+
 int pa_seed_cache_add(pa_engine* e, const uint32_t* seed_words, uint32_t n, uint32_t v, uint32_t flags,
                       int32_t* seed_id) {
     if (!e || !seed_words || !seed_id) return PA_ERR_INVALID_ARG;

@@ -162,3 +162,21 @@ def test_served_admission_evicts_idle_slots_within_budget(torch_cuda, engine):
     with pytest.raises(pa.PAError) as ei:
         engine.submit(job)
     assert ei.value.code == pa.PA_ERR_TOO_LARGE
+
+
+def test_pool_reserve_then_serve(torch_cuda, engine):
+    """Reserved slots exist before any request: a budget for two 2^20-bit slots gives two; requests
+    served afterwards still equal the same request alone."""
+    per_slot = int(12.625 * (1 << 20)) + 8192
+    engine.set_pool(hbm_budget_bytes=2 * per_slot + 4096, max_slots=8)
+    assert engine.pool_reserve(1 << 20, 5) == 2
+    assert engine.pool_reserve(1 << 20, 1) == 2  # already there
+    with pytest.raises(pa.PAError):
+        engine.pool_reserve(3 << 18, 1)  # not a power of two
+    reqs = W.poisson_requests(rate=3000, count=12, lo=14, hi=20, rng_seed=21)
+    words = max(r.n // 32 + max(r.seed_word0, r.key_word0) for r in reqs) + 64
+    banks = W.HostBanks(words)
+    res = W.serve(engine, reqs, banks, out_slots=3, keep=lambda r: True)
+    for r in reqs:
+        want = alone(engine, banks.seed_words(r), banks.key_start(r), banks.key_rest(r), r.n, r.v, r.flags)
+        assert np.array_equal(res.outputs[r.rid], want), r
