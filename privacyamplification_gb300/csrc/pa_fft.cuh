@@ -108,6 +108,29 @@ __device__ __forceinline__ void stage(float2 (&x)[E], const float2* w) {
     }
 }
 
+// Twiddle table of a stage (radix R, NS): tab[r * NS + m] = W_{NS R}^{DIR m r}, m < NS, r < R, filled
+// by all threads of the block.  Laid out by r so that a warp's lanes (consecutive j, so consecutive
+// m = j mod NS) read consecutive entries.
+template <int R, int NS, int DIR>
+__device__ __forceinline__ void fill_stage_table(float2* tab) {
+    for (int i = threadIdx.x; i < R * NS; i += blockDim.x) tab[i] = unit_root<DIR>((i % NS) * (i / NS), NS * R);
+}
+
+// Stage compute with the twiddles read from a table made by fill_stage_table (instead of the power
+// ladder of `stage`), then radix-R DFTs of the thread's butterflies (map Map over sequences of L).
+template <int R, int NS, int DIR, int E, int L, class Map>
+__device__ __forceinline__ void stage_tab(float2 (&x)[E], const float2* tab) {
+#pragma unroll
+    for (int q = 0; q < E / R; ++q) {
+        int seq, j;
+        Map::template at<L, R>(q, seq, j);
+        const float2* tq = tab + (j % NS);
+#pragma unroll
+        for (int r = 1; r < R; ++r) x[q * R + r] = cmul(x[q * R + r], tq[r * NS]);
+        dft<R, DIR>(reinterpret_cast<float2(&)[R]>(x[q * R]));
+    }
+}
+
 // Twiddle bases of a stage for the thread's butterflies: w[q] = W_{NS R}^{DIR (j_q mod NS)}.
 template <int L, int R, int NS, int DIR, int E, class Map>
 __device__ __forceinline__ void stage_bases(float2* w) {

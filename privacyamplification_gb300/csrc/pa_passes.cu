@@ -635,6 +635,7 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* sm = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     __shared__ float2 tws[(QB > 0 ? QB : 1) + QL][NT];
+    __shared__ float2 tab2[P::NSTAGE == 2 ? P::RB * 16 : 1];  // second-stage twiddles
     __shared__ float redf[32];
     __shared__ __align__(8) uint64_t bar;
     __shared__ int s_fail;
@@ -657,6 +658,7 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
         }
 #pragma unroll
         for (int q = 0; q < QL; ++q) tws[(QB > 0 ? QB : 1) + q][t] = w[q];
+        if (P::NSTAGE == 2) fill_stage_table<P::RB, 16, +1>(tab2);
     }
     float corr;
     {
@@ -736,7 +738,7 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
                 exchange<L, SP, 4, E, 16, 1, MapMirrorRow, P::RB, Lin>(x, sm);
 #pragma unroll
                 for (int q = 0; q < QB; ++q) w[q] = tws[q][t];
-                stage<P::RB, 16, +1, E>(x, w);
+                stage_tab<P::RB, 16, +1, E, L, Lin>(x, tab2);
                 exchange<L, SP, 4, E, P::RB, 16, Lin, RL, Lin>(x, sm);
             } else {
                 exchange<L, SP, 4, E, 16, 1, MapMirrorRow, RL, Lin>(x, sm);
