@@ -180,3 +180,20 @@ def test_pool_reserve_then_serve(torch_cuda, engine):
     for r in reqs:
         want = alone(engine, banks.seed_words(r), banks.key_start(r), banks.key_rest(r), r.n, r.v, r.flags)
         assert np.array_equal(res.outputs[r.rid], want), r
+
+
+def test_pool_refuses_blocks_beyond_one_fp32_pass(torch_cuda, engine):
+    """Batches and served blocks run single-pass FP32 blocks (n <= 2^27); larger ones (pa_process's
+    chunked path) are refused before any work is queued."""
+    n, v = 1 << 28, (1 << 26) + (1 << 25)
+    d = torch_cuda.zeros(16, dtype=torch_cuda.int32, device="cuda")
+    p = d.data_ptr()
+    job = pa.PAJob(p, -1, p, p, n, v, DEFAULT, p)
+    with pytest.raises(pa.PAError) as ei:
+        engine.batch_run([job])
+    assert ei.value.code == pa.PA_ERR_TOO_LARGE
+    host = np.zeros(4, np.uint32)
+    hjob = pa.PAJob(host.ctypes.data, -1, host.ctypes.data, host.ctypes.data, n, v, DEFAULT, host.ctypes.data)
+    with pytest.raises(pa.PAError) as ei:
+        engine.submit(hjob)
+    assert ei.value.code == pa.PA_ERR_TOO_LARGE
