@@ -122,6 +122,13 @@ PA_API int pa_stage_times(pa_engine* e, float* ms, int max_stages, int* nstages,
 PA_API const char* pa_error_string(int code);
 PA_API int pa_last_cuda_error(pa_engine* e);
 
+/* Self-test of the failure path (no counterpart in the reference, whose kernels have no bounded
+ * waits): runs one CTA whose mbarrier wait is never satisfied, with a limit of `rounds` try_wait rounds
+ * (1..2^20), and stores the device error word in *status: 1 = the wait expired and was reported, as a
+ * TMA wait of the three-pass kernels does (pa_process then returns PA_ERR_CUDA with
+ * cudaErrorLaunchTimeout in pa_last_cuda_error).  The context stays usable afterwards. */
+PA_API int pa_selftest_wait_timeout(int32_t device_id, uint32_t rounds, int32_t* status);
+
 /* ---- Batched and served blocks -------------------------------------------------------------------
  * No counterpart in the reference: its mainloop (PrivacyAmplification.cu:1686-2118) runs one block at
  * a time with a host sync after every step.  Here blocks of different sizes run concurrently on a pool

@@ -41,7 +41,7 @@ EXPORTS = ("pa_create", "pa_destroy", "pa_set_seed", "pa_process", "pa_set_seed_
            "pa_sync", "pa_key_split", "pa_output_bytes", "pa_kernels_per_block", "pa_set_timing",
            "pa_stage_times", "pa_error_string", "pa_last_cuda_error", "pa_process_noalloc", "pa_set_pool",
            "pa_seed_cache_add", "pa_seed_cache_clear", "pa_batch_run", "pa_batch_sync", "pa_submit", "pa_poll",
-           "pa_set_split", "pa_get_split", "pa_autotune", "pa_pool_reserve")
+           "pa_set_split", "pa_get_split", "pa_autotune", "pa_pool_reserve", "pa_selftest_wait_timeout")
 
 
 class PAError(RuntimeError):
@@ -120,6 +120,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pa_get_split": ([eng, ctypes.c_uint32], ctypes.c_int),
         "pa_autotune": ([eng, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
         "pa_pool_reserve": ([eng, ctypes.c_uint32, ctypes.c_int32], ctypes.c_int),
+        "pa_selftest_wait_timeout": ([ctypes.c_int32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -149,6 +150,15 @@ def process_noalloc(d_seed: int, d_key_start: int, d_key_rest: int, n: int, v: i
                                            stream or None)
     if rc != 0:
         raise PAError(rc, "pa_process_noalloc")
+
+
+def selftest_wait_timeout(device_id: int = 0, rounds: int = 4096) -> int:
+    """Runs a bounded device wait that is never satisfied; returns the device error word (1 = expired)."""
+    st = ctypes.c_int32()
+    rc = load_library().pa_selftest_wait_timeout(device_id, rounds, ctypes.byref(st))
+    if rc != 0:
+        raise PAError(rc, "pa_selftest_wait_timeout")
+    return st.value
 
 
 def _u32(a) -> np.ndarray:
