@@ -552,9 +552,23 @@ def run_dynamic27(args):
         ev1.synchronize()
     st = eng.sync(check=False)
     t = ev0.elapsed_time(ev1) / 1e3
-    _line(METRIC, args.steps * N_BITS / t / 1e9, UNIT, args.steps, args.warmup, t / args.steps * 1e3,
-          "n=2^27 (h=83886080, v=50331648), dynamic seed: a fresh seed spectrum every block, do_xor, do_compress",
-          {"max_residual": st.max_residual, "clocks": clk.summary(),
+    # the same blocks, IN_FLIGHT at a time (each job brings its own seed; pa_batch_run over slots)
+    outs = [torch.empty(V_BITS // 32, dtype=torch.int32, device=dev) for _ in range(8)]
+    jobs = [pa.PAJob(seeds[i % len(seeds)].data_ptr(), -1, keys[i % len(keys)][0].data_ptr(),
+                     keys[i % len(keys)][1].data_ptr(), N_BITS, V_BITS, pa.DEFAULT_FLAGS, outs[i % 8].data_ptr())
+               for i in range(args.steps)]
+    eng.set_pool(0, 16, IN_FLIGHT)
+    eng.batch_run(jobs[: args.warmup], 0, stream.cuda_stream)
+    eng.batch_sync(args.warmup)
+    with ClockSampler(0) as clk2:
+        eng.batch_run(jobs, 0, stream.cuda_stream)
+        bst = eng.batch_sync(args.steps)
+    t2 = bst[0].gpu_ms / 1e3
+    _line(METRIC, args.steps * N_BITS / t2 / 1e9, UNIT, args.steps, args.warmup, t2 / args.steps * 1e3,
+          "n=2^27 (h=83886080, v=50331648), dynamic seed: a fresh seed spectrum every block, do_xor, do_compress; "
+          "%d blocks in flight" % IN_FLIGHT,
+          {"max_residual": max(st.max_residual, max(x.max_residual for x in bst)), "clocks": clk2.summary(),
+           "value_one_stream": args.steps * N_BITS / t / 1e9, "clocks_one_stream": clk.summary(),
            "gpu_launches": args.steps * (3 + pa.kernels_per_block(N_BITS, V_BITS))})
     eng.close()
 
