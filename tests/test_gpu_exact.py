@@ -149,3 +149,26 @@ def test_chunked_guard_falls_back_to_exact(big_engine):
     for r0 in (0, v // 2 // 64 * 64, v - 64):
         assert np.array_equal(np.unpackbits(out[r0 // 8: r0 // 8 + 8]), blk.rows(r0, r0 + 64) ^ krb[r0: r0 + 64])
     blk.close()
+
+
+def test_maximum_size_2p30(pa_lib):
+    """The largest block the engine accepts, n = 2^30 (66 chunk blocks): sampled rows against the
+    direct oracle, and the key_rest XOR; n = 2^30 + 1024 is refused."""
+    n, v = std_sizes(1 << 30)
+    rng = np.random.default_rng(30)
+    seed = rng.integers(0, 1 << 32, n // 32, dtype=np.uint64).astype(np.uint32)
+    recv = rng.integers(0, 1 << 32, n // 32 + 1, dtype=np.uint64).astype(np.uint32)
+    ks, kr = pa.key_split(recv, n, v)
+    with pa.Engine(max_sample_size=n) as eng:
+        eng.set_seed(seed, n, -1)
+        out = eng.process(ks, kr, n, v)
+        assert eng.last_stats.exact == 2 and eng.last_stats.max_residual < 0.1
+        plain = eng.process(ks, kr, n, v, pa.FLAG_COMPRESS)
+        assert np.array_equal(out, plain ^ kr.astype(">u4").view(np.uint8))
+        with pytest.raises(pa.PAError):
+            eng.set_seed(np.zeros((n + 1024) // 32, np.uint32), n + 1024, -1)
+    blk = O.DirectBlock(seed, ks, n, v)
+    krb = O.bits_msb(kr, v).astype(np.uint8)
+    for r0 in (0, 64 * 1234567, v - 64):
+        assert np.array_equal(np.unpackbits(out[r0 // 8: r0 // 8 + 8]), blk.rows(r0, r0 + 64) ^ krb[r0: r0 + 64]), r0
+    blk.close()
