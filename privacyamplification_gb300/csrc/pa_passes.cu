@@ -622,7 +622,11 @@ __global__ void __launch_bounds__(256, 2)
 // (256 tiles x 1 row x CPT/2 pairs) gather it into shared memory in pair order (float4 p = pair p),
 // or cooperative loads when a tile row is too wide for a box.  The next row's copy starts as soon as
 // the last exchange of the current row has finished with the buffer.
-template <int LOGL>
+// KEEP8: the last stage's outputs r < KEEP8 * RL / 8 (samples m2 = j + NSL r) are the only ones that can
+// fall below out_bits; the others are neither rounded nor stored, and the compiler drops their share of
+// the last radix stage.  Their plane words keep whatever the buffer held: k_finish never reads a word
+// past out_bits.
+template <int LOGL, int KEEP8>
 __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     k_pass_c(const __grid_constant__ CUtensorMap mapZ, const float2* __restrict__ Z, BlockGeom g,
              const unsigned long long* cnt, uint32_t* __restrict__ planes, unsigned int* resid_bits, int* err) {
@@ -630,6 +634,8 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     using P = Plan<LOGL>;
     using Lin = MapLinear<NT>;
     constexpr int RL = P::RA, NSL = L / RL;
+    constexpr int KR = KEEP8 * RL / 8;
+    static_assert(KEEP8 >= 1 && KEEP8 <= 8 && KR * 8 == KEEP8 * RL, "KEEP8 must split the last radix evenly");
     constexpr int QB = P::NSTAGE == 2 ? E / P::RB : 0;
     constexpr int QL = E / RL;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -751,18 +757,21 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
             for (int q = 0; q < QL; ++q) w[q] = tws[(QB > 0 ? QB : 1) + q][t];
             stage<RL, (P::NSTAGE == 2 ? 16 * P::RB : 16), +1, E>(x, w);
         }
-        // outputs: butterfly u = t + q*NT (j = u), sample m2 = j + NSL*r; lanes hold consecutive m2
+        // outputs: butterfly u = t + q*NT (j = u), sample m2 = j + NSL*r; lanes hold consecutive m2.
+        // Sample x = 2 (m1 + N1 m2) + tt is below out_bits iff m2 < lim[tt] = ceil((out_bits - 2 m1 - tt) / 2N1).
+        const uint32_t two_m1 = 2u * m1, span = 2u << g.log_n1;
+        const uint32_t lim0 = g.out_bits > two_m1 ? (g.out_bits - two_m1 + span - 1u) >> (g.log_n1 + 1) : 0u;
+        const uint32_t lim1 = g.out_bits > two_m1 + 1u ? (g.out_bits - two_m1 - 1u + span - 1u) >> (g.log_n1 + 1) : 0u;
 #pragma unroll
         for (int q = 0; q < QL; ++q) {
             const int j = t + q * NT;
 #pragma unroll
-            for (int r = 0; r < RL; ++r) {
+            for (int r = 0; r < KR; ++r) {
                 const uint32_t m2 = (uint32_t)(j + NSL * r);
-                const uint64_t x0 = 2ull * ((uint64_t)m1 + ((uint64_t)m2 << g.log_n1));
                 const float2 v = x[q * RL + r];
                 const float v0 = v.x + corr, v1 = v.y + corr;
                 const float r0 = rintf(v0), r1 = rintf(v1);
-                const bool ok0 = x0 < g.out_bits, ok1 = x0 + 1 < g.out_bits;
+                const bool ok0 = m2 < lim0, ok1 = m2 < lim1;
                 if (ok0) res = fmaxf(res, fabsf(v0 - r0));
                 if (ok1) res = fmaxf(res, fabsf(v1 - r1));
                 const uint32_t be = __ballot_sync(0xffffffffu, ok0 && ((int)r0 & 1));
@@ -866,14 +875,38 @@ static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2*
     return (int)cudaGetLastError();
 }
 
-template <int LOGL>
-static int pass_c_l(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
+template <int LOGL, int KEEP8>
+static int pass_c_k(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
                     uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s) {
     constexpr int NT = (1 << LOGL) / 32;
     size_t smem = (size_t)TileStride<(1 << LOGL)>::value * sizeof(float2) + 128;  // + TMA alignment
-    smem_attr(k_pass_c<LOGL>, smem);
-    k_pass_c<LOGL><<<grid_units(1u << g.log_n1, num_sms), NT, smem, s>>>(maps.z, Z, g, cnt, planes, resid, err);
+    smem_attr(k_pass_c<LOGL, KEEP8>, smem);
+    k_pass_c<LOGL, KEEP8><<<grid_units(1u << g.log_n1, num_sms), NT, smem, s>>>(maps.z, Z, g, cnt, planes, resid,
+                                                                               err);
     return (int)cudaGetLastError();
+}
+
+// Eighths of the last stage's outputs that hold samples below out_bits: samples m2 < ceil(out_bits / 2N1)
+// of every row, in last-stage output groups of NSL.
+static int pass_c_keep8(const BlockGeom& g, int rl) {
+    const uint64_t lim = ((uint64_t)g.out_bits + (2ull << g.log_n1) - 1ull) >> (g.log_n1 + 1);
+    const uint64_t nsl = (1ull << g.log_n2) / (uint64_t)rl;
+    const uint64_t live = (lim + nsl - 1ull) / nsl;  // last-stage outputs r < live
+    return (int)((live * 8ull + (uint64_t)rl - 1ull) / (uint64_t)rl);
+}
+
+// Long rows (the large blocks) have variants for 2/8, 3/8 (v = 3n/8) and 4/8 (n/2 outputs); short rows
+// and every other ratio run the full last stage.
+template <int LOGL>
+static int pass_c_l(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
+                    uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s) {
+    const int k8 = pass_c_keep8(g, Plan<LOGL>::RA);
+    if constexpr (LOGL >= 12) {
+        if (k8 <= 2) return pass_c_k<LOGL, 2>(g, maps, Z, cnt, planes, resid, err, num_sms, s);
+        if (k8 == 3) return pass_c_k<LOGL, 3>(g, maps, Z, cnt, planes, resid, err, num_sms, s);
+        if (k8 == 4) return pass_c_k<LOGL, 4>(g, maps, Z, cnt, planes, resid, err, num_sms, s);
+    }
+    return pass_c_k<LOGL, 8>(g, maps, Z, cnt, planes, resid, err, num_sms, s);
 }
 
 #define PA_ROWS_DISPATCH(LG, CALL)                   \
