@@ -133,6 +133,57 @@ __global__ void __launch_bounds__(256) k_bit_rows(const uint32_t* __restrict__ s
     rows[(size_t)(16u * a + (uint32_t)(lane & 15)) * (n2 / 16u) + 2u * c + (uint32_t)(lane >> 4)] = w;
 }
 
+// Tiled form for N1, N2 >= 256 (the large blocks): a CTA moves a 256 x 256 block of 2-bit elements,
+// input rows m2 (16 words of 16 m1 each, 64-byte segments) into shared memory, half-warp 16 x 16
+// transposes from there, and output rows m1 (16 words of 16 m2 each) back out -- every global access
+// is a 64-byte run instead of one word per row.  Rows padded to 17 words keep the column reads of the
+// transpose on distinct banks.  SEED: only for Np == n (the padded seed placement uses k_bit_rows).
+template <bool SEED>
+__global__ void __launch_bounds__(256) k_bit_rows_tiled(const uint32_t* __restrict__ src, BlockGeom g,
+                                                        uint32_t* __restrict__ rows) {
+    __shared__ uint32_t tile[256][17];  // [m2 - m20][a - a0], then [m1 - 16 a0][(m2 - m20) / 16]
+    const int t = threadIdx.x, lane = t & 31;
+    const uint32_t win = (1u << g.log_n1) / 16u, wout = (1u << g.log_n2) / 16u;  // words per input / output row
+    const uint32_t a0 = blockIdx.x * 16u, m20 = blockIdx.y * 256u;
+    // all 16 loads of the thread are issued before the first is used: one memory round trip
+    uint32_t v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int r = (t >> 4) + 16 * i, w = t & 15;
+        const uint64_t word = (uint64_t)(m20 + (uint32_t)r) * win + a0 + (uint32_t)w;
+        const uint64_t x0 = 32ull * word;  // first sample of the word
+        v[i] = (SEED || x0 <= g.h) ? __ldg(src + word) : 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int r = (t >> 4) + 16 * i, w = t & 15;
+        const uint64_t x0 = 32ull * ((uint64_t)(m20 + (uint32_t)r) * win + a0 + (uint32_t)w);
+        if (!SEED && x0 <= g.h && x0 + 31 > g.h) v[i] &= ~(0xFFFFFFFFu >> (uint32_t)(g.h - x0 + 1));
+        tile[r][w] = v[i];
+    }
+    __syncthreads();
+    // half-warp hw takes 16 x 16 blocks (cb, w): input words of m2 = m20 + 16 cb + L, column a0 + w;
+    // the results wait in registers until every input word is read, then reuse the tile (one tile per
+    // CTA keeps the whole grid resident in one wave)
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int b = (t >> 4) + 16 * i, cb = b >> 4, w = b & 15, L = lane & 15;
+        v[i] = transpose16x2(tile[16 * cb + L][w], lane);  // row m1 = 16 (a0 + w) + L
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int b = (t >> 4) + 16 * i, cb = b >> 4, w = b & 15, L = lane & 15;
+        tile[16 * w + L][cb] = v[i];
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int i = 0; i < 16; ++i) {
+        const int r = (t >> 4) + 16 * i, w = t & 15;
+        rows[(size_t)(16u * a0 + (uint32_t)r) * wout + m20 / 16u + (uint32_t)w] = tile[r][w];
+    }
+}
+
 // ============================================================================ pass A
 // Row m1: FFT over m2 of the 2N2 bits of the row, 4-step twiddle W_N^{m1 k2}, pair-order store.
 // Radices RA, RB (linear) then 16 (mirror, NS = L/16).
@@ -819,6 +870,62 @@ __global__ void __launch_bounds__(1024) k_finish(const uint32_t* __restrict__ pl
     }
 }
 
+// Tiled form for N1 >= 256: a CTA takes plane rows m1 = m10 .. m10+255 and plane word columns
+// c0 .. c0+7 (m2 = 32 c0 .. 32 c0 + 255).  Plane words arrive as 32-byte row segments, the half-warp
+// transposes of k_finish run on shared memory, and each m2 leaves as 16 consecutive output words
+// (64 bytes), with key_rest read the same way.
+__global__ void __launch_bounds__(256) k_finish_tiled(const uint32_t* __restrict__ planes, BlockGeom g,
+                                                      const uint32_t* __restrict__ key_rest, uint32_t flags,
+                                                      uint32_t* __restrict__ out, uint32_t nwords) {
+    __shared__ uint32_t se[256][9], so[256][9];  // [m1 - m10][c - c0], even / odd samples
+    __shared__ uint32_t sw[256][17];             // [m2 - 32 c0][(m1 - m10) / 16]
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t n1 = 1u << g.log_n1, wpr = (1u << g.log_n2) / 32u;
+    const size_t plane_words = (size_t)n1 * wpr;
+    const uint32_t m10 = blockIdx.x * 256u, c0 = blockIdx.y * 8u;
+    // Every load of the thread (16 plane words, and the 16 key_rest words its output words XOR with) is
+    // issued before the first is used: one memory round trip per CTA.
+    uint32_t pv[16], kr[16];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int r = (t >> 3) + 32 * i, w = t & 7;
+        const uint32_t c = c0 + (uint32_t)w;
+        const size_t off = (size_t)(m10 + (uint32_t)r) * wpr + c;
+        pv[2 * i] = c < wpr ? __ldg(planes + off) : 0u;
+        pv[2 * i + 1] = c < wpr ? __ldg(planes + plane_words + off) : 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int ml = (t >> 4) + 16 * i, j = t & 15;
+        const uint64_t ow = ((32ull * c0 + (uint64_t)ml) * n1 + m10) / 16ull + (uint64_t)j;
+        kr[i] = ((flags & kXor) && ow < nwords && 32ull * ow < g.v) ? __ldg(key_rest + ow) : 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int r = (t >> 3) + 32 * i, w = t & 7;
+        se[r][w] = pv[2 * i];
+        so[r][w] = pv[2 * i + 1];
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int i = 0; i < 8; ++i) {
+        const int u = warp + 8 * i, al = u >> 3, cl = u & 7;  // rows 32 al + lane, word column cl
+        const uint32_t ve = se[32 * al + lane][cl], vo = so[32 * al + lane][cl];
+        const uint32_t lo = transpose16x2(msb_pairs(ve, vo), lane);
+        const uint32_t hi = transpose16x2(msb_pairs(ve >> 16, vo >> 16), lane);
+        const int L = lane & 15, h = lane >> 4;
+        sw[32 * cl + L][2 * al + h] = lo;        // m2 = 32 (c0 + cl) + L, rows m10 + 32 al + 16 h ...
+        sw[32 * cl + 16 + L][2 * al + h] = hi;   // m2 + 16
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int ml = (t >> 4) + 16 * i, j = t & 15;
+        const uint64_t ow = ((32ull * c0 + (uint64_t)ml) * n1 + m10) / 16ull + (uint64_t)j;
+        if (ow < nwords) out[ow] = __byte_perm(sw[ml][j] ^ kr[i], 0, 0x0123);
+    }
+}
+
 // ============================================================================ launchers
 template <class K>
 static void smem_attr(K k, size_t bytes) {
@@ -831,6 +938,12 @@ static int grid_units(uint32_t units, int num_sms) {
 
 int launch_bit_rows(const BlockGeom& g, const uint32_t* bits, bool seed, uint32_t* rows, cudaStream_t s) {
     const uint32_t n1 = 1u << g.log_n1, n2 = 1u << g.log_n2;
+    if (n1 >= 256u && n2 >= 256u && (!seed || (1u << g.log_np) == g.n)) {
+        dim3 grid(n1 / 256u, n2 / 256u);
+        if (seed) k_bit_rows_tiled<true><<<grid, 256, 0, s>>>(bits, g, rows);
+        else k_bit_rows_tiled<false><<<grid, 256, 0, s>>>(bits, g, rows);
+        return (int)cudaGetLastError();
+    }
     dim3 grid((n1 / 16u + 7u) / 8u, n2 / 32u);
     if (seed) k_bit_rows<true><<<grid, 256, 0, s>>>(bits, g, rows);
     else k_bit_rows<false><<<grid, 256, 0, s>>>(bits, g, rows);
@@ -1000,6 +1113,11 @@ int launch_finish(const BlockGeom& g, const uint32_t* planes, const uint32_t* ke
     // only plane columns that hold output samples: m2 < ceil(out_bits / (2 N1))
     const uint32_t m2max = (uint32_t)(((uint64_t)g.out_bits + 2ull * n1 - 1ull) / (2ull * n1));
     const uint32_t cols = std::min<uint32_t>(wpr, (m2max + 31u) / 32u);
+    if (n1 >= 256u) {
+        dim3 grid(n1 / 256u, (cols + 7u) / 8u);
+        k_finish_tiled<<<grid, 256, 0, s>>>(planes, g, key_rest, flags, out, nwords);
+        return (int)cudaGetLastError();
+    }
     dim3 grid((n1 / 32u + 3u) / 4u, (cols + 7u) / 8u);
     k_finish<<<grid, 1024, 0, s>>>(planes, g, key_rest, flags, out, nwords);
     return (int)cudaGetLastError();

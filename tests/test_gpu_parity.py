@@ -70,6 +70,25 @@ def test_large_pow2_vs_ntt(gpu_engine, logn):
     assert np.array_equal(out, O.ntt(seed, ks, kr, n, v, DEFAULT))
 
 
+# n = 2^22 runs rows of 2^14 (last inverse stage radix 32 over 512 butterflies, columns of 2^7): pass C
+# rounds only the last-stage outputs r < 32 * KEEP8 / 8 that can hold samples below out_bits, with
+# KEEP8 = 2, 3, 4 or 8.  These v sit on and just past each boundary (live outputs r = ceil(v / 2^17)).
+@pytest.mark.parametrize("v,flags,split", [
+    (1 << 20, DEFAULT, 0), ((1 << 20) + 32, DEFAULT, 0), (3 << 19, DEFAULT, 0), ((3 << 19) + 32, DEFAULT, 0),
+    ((1 << 21) - 32, pa.FLAG_COMPRESS, 0), (3 << 19, 0, 0), ((1 << 21) + 32, DEFAULT, 0), (32, DEFAULT, 0),
+    ((3 << 19) + 32, DEFAULT, 12), ((1 << 20) + 32, DEFAULT, 13)])
+def test_pass_c_output_share_variants(gpu_engine, v, flags, split):
+    n = 1 << 22
+    if split:
+        gpu_engine.set_split(21, split)
+    try:
+        seed, ks, kr, out = run_block(gpu_engine, n, v, v + flags, flags)
+    finally:
+        if split:
+            gpu_engine.set_split(21, 14)
+    assert np.array_equal(out, O.ntt(seed, ks, kr, n, v, flags))
+
+
 @pytest.mark.parametrize("n,v,flags", [
     (1 << 16, 24576, 0), (1 << 16, 24576, pa.FLAG_COMPRESS), (1 << 16, 24576, pa.FLAG_XOR_KEY_REST),
     (1 << 16, 61440, DEFAULT), (1 << 16, 32, DEFAULT), (1 << 16, 65504, DEFAULT), (1 << 16, 32768, 0),
