@@ -671,8 +671,12 @@ __global__ void __launch_bounds__(256, 2)
 // Row m1: inverse FFT over k2 (radices 16, RB, RA), + correction, round, parity bit planes.
 // Input: Z, tile-major from pass B.  Row m1 is the CPT/2 pairs of row m1 of every tile; 3D TMA boxes
 // (256 tiles x 1 row x CPT/2 pairs) gather it into shared memory in pair order (float4 p = pair p),
-// or cooperative loads when a tile row is too wide for a box.  The next row's copy starts as soon as
-// the last exchange of the current row has finished with the buffer.
+// or cooperative loads when a tile row is too wide for a box.  Shared memory holds [row boxes 0 ..
+// early-1][exchange buffer], so a row occupies the first `early` boxes' own space and the start of the
+// exchange buffer.  The next row's first `early` boxes are gathered as soon as the current row has been
+// read into registers (under the whole row's transform); the rest as soon as the last exchange has
+// finished with the buffer.  `early` is as many boxes as shared memory holds (all of them for rows up to
+// 2^13; 19 of 32 for rows of 2^14).
 // KEEP8: the last stage's outputs r < KEEP8 * RL / 8 (samples m2 = j + NSL r) are the only ones that can
 // fall below out_bits; the others are neither rounded nor stored, and the compiler drops their share of
 // the last radix stage.  Their plane words keep whatever the buffer held: k_finish never reads a word
@@ -680,7 +684,8 @@ __global__ void __launch_bounds__(256, 2)
 template <int LOGL, int KEEP8>
 __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     k_pass_c(const __grid_constant__ CUtensorMap mapZ, const float2* __restrict__ Z, BlockGeom g,
-             const unsigned long long* cnt, uint32_t* __restrict__ planes, unsigned int* resid_bits, int* err) {
+             const unsigned long long* cnt, uint32_t* __restrict__ planes, unsigned int* resid_bits, int* err,
+             int early) {
     constexpr int L = 1 << LOGL, NT = L / 32, E = 32, LR = L / 16, SP = TileStride<L>::value;
     using P = Plan<LOGL>;
     using Lin = MapLinear<NT>;
@@ -690,11 +695,10 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     constexpr int QB = P::NSTAGE == 2 ? E / P::RB : 0;
     constexpr int QL = E / RL;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float2* sm = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     __shared__ float2 tws[(QB > 0 ? QB : 1) + QL][NT];
     __shared__ float2 tab2[P::NSTAGE == 2 ? P::RB * 16 : 1];  // second-stage twiddles
     __shared__ float redf[32];
-    __shared__ __align__(8) uint64_t bar;
+    __shared__ __align__(8) uint64_t bar, bar_late;  // TMA completion: boxes [0, early), [early, nb)
     __shared__ int s_fail;
     const uint32_t n1 = 1u << g.log_n1;
     const int cpt = 8192 >> g.log_n1;               // pass B tile width (columns)
@@ -702,6 +706,10 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     const int ntiles = (int)(L / cpt);
     const bool tma = cpt <= 128;
     const int boxt = ntiles < 256 ? ntiles : 256;   // tiles per box
+    const int nb = ntiles / boxt;                   // boxes per row
+    if (!tma) early = 0;
+    float2* srow = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    float2* sm = srow + (size_t)early * boxt * cpt;  // exchange buffer
     const int t = threadIdx.x, lane = t & 31;
     {
         float2 w[4];
@@ -725,28 +733,42 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     }
     // rows holding at least one output sample: m1 < min(N1, ceil(out_bits / 2))
     const uint32_t rows_out = (uint32_t)(((uint64_t)g.out_bits + 1ull) / 2ull < n1 ? (g.out_bits + 1u) / 2u : n1);
-    auto load_row = [&](uint32_t r) {
+    const uint32_t box_bytes = (uint32_t)(boxt * cpt * sizeof(float2));
+    auto load_early = [&](uint32_t r) {  // boxes [0, early) of row r (TMA only)
+        if (r >= rows_out || early == 0 || t != 0) return;
+        mbar_expect_tx(&bar, (uint32_t)early * box_bytes);
+#pragma unroll 1
+        for (int b = 0; b < early; ++b) tma_load_3d(srow + (size_t)b * boxt * cpt, &mapZ, 0, (int)r, boxt * b, &bar);
+    };
+    auto load_late = [&](uint32_t r) {  // boxes [early, nb) of row r, or the whole row by cooperative loads
         if (r >= rows_out) return;
         if (tma) {
-            if (t == 0) {
-                mbar_expect_tx(&bar, (uint32_t)(L * sizeof(float2)));
+            if (early == nb || t != 0) return;
+            mbar_expect_tx(&bar_late, (uint32_t)(nb - early) * box_bytes);
 #pragma unroll 1
-                for (int b = 0; b < ntiles / boxt; ++b)
-                    tma_load_3d(sm + (size_t)b * boxt * cpt, &mapZ, 0, (int)r, boxt * b, &bar);
-            }
+            for (int b = early; b < nb; ++b)
+                tma_load_3d(srow + (size_t)b * boxt * cpt, &mapZ, 0, (int)r, boxt * b, &bar_late);
         } else {
             const float4* z4 = reinterpret_cast<const float4*>(Z);
-            float4* s4 = reinterpret_cast<float4*>(sm);
+            float4* s4 = reinterpret_cast<float4*>(srow);
             for (int p = t; p < L / 2; p += NT) {
                 int tl = p / pairs_per_tile, cp = p % pairs_per_tile;
                 s4[p] = __ldcs(z4 + ((size_t)tl * n1 + r) * pairs_per_tile + cp);
             }
         }
     };
-    uint32_t parity = 0;
+    auto wait_bar = [&](uint64_t* b, uint32_t& parity) {
+        if (!s_fail && !mbar_wait(b, parity)) {
+            s_fail = 1;
+            atomicExch(err, kErrTmaTimeout);
+        }
+        parity ^= 1u;
+    };
+    uint32_t parity = 0, parity_late = 0;
     if (t == 0) {
         s_fail = 0;
         mbar_init(&bar, 1);
+        mbar_init(&bar_late, 1);
     }
     __syncthreads();
     const size_t plane_words = (size_t)n1 * (L / 32);
@@ -754,21 +776,19 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     for (uint32_t m1 = rows_out + blockIdx.x; m1 < n1; m1 += gridDim.x)
         for (int w = t; w < L / 32; w += NT) planes[(size_t)m1 * (L / 32) + w] = planes[plane_words + (size_t)m1 * (L / 32) + w] = 0u;
     fence_proxy_async();
-    load_row(blockIdx.x);
+    load_early(blockIdx.x);
+    load_late(blockIdx.x);
     float res = 0.f;
     for (uint32_t m1 = blockIdx.x; m1 < rows_out; m1 += gridDim.x) {
         uint32_t* pe = planes + (size_t)m1 * (L / 32);
         uint32_t* po = pe + plane_words;
         if (tma) {
-            if (!s_fail && !mbar_wait(&bar, parity)) {
-                s_fail = 1;
-                atomicExch(err, kErrTmaTimeout);
-            }
-            parity ^= 1u;
+            if (early > 0) wait_bar(&bar, parity);
+            if (early < nb) wait_bar(&bar_late, parity_late);
         }
-        __syncthreads();  // row in sm
+        __syncthreads();  // row in shared memory
         float2 x[E];
-        const float4* row4 = reinterpret_cast<const float4*>(sm);
+        const float4* row4 = reinterpret_cast<const float4*>(srow);
         if (t != 0) {
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
@@ -788,6 +808,11 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
                 x[16 + 15 - r] = make_float2(b.z, b.w);
             }
         }
+        if (early > 0) {  // the row's own boxes are read: gather the next row's under this row's transform
+            __syncthreads();
+            fence_proxy_async();
+            load_early(m1 + gridDim.x);
+        }
         stage<16, 1, +1, E>(x, nullptr);
         {
             float2 w[4];
@@ -800,10 +825,10 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
             } else {
                 exchange<L, SP, 4, E, 16, 1, MapMirrorRow, RL, Lin>(x, sm);
             }
-            // sm is free: start the next row's copy under the last stage
+            // the exchange buffer is free: the rest of the next row's copy runs under the last stage
             __syncthreads();
             fence_proxy_async();
-            load_row(m1 + gridDim.x);
+            load_late(m1 + gridDim.x);
 #pragma unroll
             for (int q = 0; q < QL; ++q) w[q] = tws[(QB > 0 ? QB : 1) + q][t];
             stage<RL, (P::NSTAGE == 2 ? 16 * P::RB : 16), +1, E>(x, w);
@@ -988,14 +1013,47 @@ static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2*
     return (int)cudaGetLastError();
 }
 
+// Per-block shared memory limit of the current device (opt-in maximum).
+static size_t smem_optin_limit() {
+    static const size_t limit = [] {
+        int dev = 0, optin = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+            return (size_t)0;
+        return (size_t)optin;
+    }();
+    return limit;
+}
+
+// Boxes of a pass C row that fit in shared memory beside the exchange buffer and the kernel's static
+// arrays (see k_pass_c); 0 for cooperative row loads or when the kernel's attributes are unknown.
+static int pass_c_early(const BlockGeom& g, int logl, size_t exch_bytes, size_t static_bytes) {
+    const uint32_t cpt = 8192u >> g.log_n1;
+    if (cpt > 128u || static_bytes == 0) return 0;
+    const uint32_t ntiles = (1u << logl) / cpt, boxt = ntiles < 256u ? ntiles : 256u;
+    const size_t box_bytes = (size_t)boxt * cpt * sizeof(float2), nb = ntiles / boxt;
+    const size_t limit = smem_optin_limit(), used = exch_bytes + static_bytes + 1024;  // 1 KB margin
+    if (limit <= used) return 0;
+    return (int)std::min<size_t>(nb, (limit - used) / box_bytes);
+}
+
 template <int LOGL, int KEEP8>
 static int pass_c_k(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
                     uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s) {
     constexpr int NT = (1 << LOGL) / 32;
-    size_t smem = (size_t)TileStride<(1 << LOGL)>::value * sizeof(float2) + 128;  // + TMA alignment
+    const size_t exch = (size_t)TileStride<(1 << LOGL)>::value * sizeof(float2) + 128;  // + TMA alignment
+    static const size_t static_bytes = [] {  // the kernel's own __shared__ arrays
+        cudaFuncAttributes fa{};
+        return cudaFuncGetAttributes(&fa, k_pass_c<LOGL, KEEP8>) == cudaSuccess ? (size_t)fa.sharedSizeBytes
+                                                                                 : (size_t)0;
+    }();
+    const int early = pass_c_early(g, LOGL, exch, static_bytes);
+    const uint32_t cpt = 8192u >> g.log_n1, ntiles = (1u << LOGL) / cpt;
+    const size_t box_bytes = (size_t)(ntiles < 256u ? ntiles : 256u) * cpt * sizeof(float2);
+    const size_t smem = exch + (size_t)early * box_bytes;
     smem_attr(k_pass_c<LOGL, KEEP8>, smem);
     k_pass_c<LOGL, KEEP8><<<grid_units(1u << g.log_n1, num_sms), NT, smem, s>>>(maps.z, Z, g, cnt, planes, resid,
-                                                                               err);
+                                                                               err, early);
     return (int)cudaGetLastError();
 }
 
