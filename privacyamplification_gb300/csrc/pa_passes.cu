@@ -196,7 +196,7 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     constexpr int QB = P::NSTAGE == 2 ? E / P::RB : 0;   // butterflies per thread in stage B
     constexpr int T1N = LR < 32 ? LR : 32, T2N = LR / T1N;  // W_N^{m1 j} = T1[j % 32] T2[j / 32]
     extern __shared__ float2 sm[];
-    __shared__ float2 rho[16], t1[T1N], t2[T2N];
+    __shared__ float2 rho[2][16], t1[2][T1N], t2[2][T2N];  // per-row tables, double-buffered like bits
     __shared__ float2 tws[(QB > 0 ? QB : 1) + 2][NT];
     __shared__ __align__(16) uint32_t bits[2][L / 16];  // double buffer: this row, next row
     __shared__ unsigned long long red[32];
@@ -222,21 +222,28 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
         if (r < n1) cp_async8(&bits[buf][2 * t], rows + (size_t)r * (L / 16) + 2 * t);
         cp_async_commit();
     };
-    fetch_row(blockIdx.x, 0);
-    int buf = 0;
-    for (uint32_t m1 = blockIdx.x; m1 < n1; m1 += gridDim.x, buf ^= 1) {
-        __syncthreads();  // previous row done with bits[buf ^ 1] / tables / sm
-        fetch_row(m1 + gridDim.x, buf ^ 1);
-        cp_async_wait_group<1>();  // this thread's copy of row m1 has landed
-        for (int i = t; i < 16 + T1N + T2N; i += NT) {  // W_N^{m1 LR r}, W_N^{m1 i}, W_N^{m1 T1N i}
+    // Row tables W_N^{m1 LR r}, W_N^{m1 i}, W_N^{m1 T1N i} of row m1 into buffer b.  Row m1 + G's are
+    // computed while row m1's first stage runs (independent work the compiler interleaves), so the few
+    // threads doing it do not hold the block at a barrier.
+    auto row_tables = [&](uint32_t m1, int b) {
+        if (m1 >= n1) return;
+        for (int i = t; i < 16 + T1N + T2N; i += NT) {
             uint64_t e = i < 16 ? (uint64_t)LR * (uint64_t)i : (i < 16 + T1N ? (uint64_t)(i - 16)
                                                                                 : (uint64_t)T1N * (uint64_t)(i - 16 - T1N));
             float2 w = expmi_pi((uint32_t)((2ull * m1 * e) & ((2ull << g.log_n) - 1)), g.log_n);
-            if (i < 16) rho[i] = w;
-            else if (i < 16 + T1N) t1[i - 16] = w;
-            else t2[i - 16 - T1N] = w;
+            if (i < 16) rho[b][i] = w;
+            else if (i < 16 + T1N) t1[b][i - 16] = w;
+            else t2[b][i - 16 - T1N] = w;
         }
-        __syncthreads();  // all copies of row m1 and the tables visible
+    };
+    fetch_row(blockIdx.x, 0);
+    row_tables(blockIdx.x, 0);
+    int buf = 0;
+    for (uint32_t m1 = blockIdx.x; m1 < n1; m1 += gridDim.x, buf ^= 1) {
+        __syncthreads();  // previous row done with bits[buf ^ 1] / tables [buf ^ 1] / sm
+        fetch_row(m1 + gridDim.x, buf ^ 1);
+        cp_async_wait_group<1>();  // this thread's copy of row m1 has landed
+        __syncthreads();  // all copies of row m1 visible
         ones += __popc(bits[buf][2 * t]) + __popc(bits[buf][2 * t + 1]);
         float2 x[E];
 #pragma unroll
@@ -250,6 +257,7 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
                 x[q * P::RA + r] = make_float2((float)((w >> (sh + 1)) & 1u), (float)((w >> sh) & 1u));
             }
         }
+        row_tables(m1 + gridDim.x, buf ^ 1);
         stage<P::RA, 1, -1, E>(x, nullptr);
         if (P::NSTAGE == 2) {
             exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm);
@@ -267,11 +275,11 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
         for (int q = 0; q < 2; ++q) {
             int seq, j;
             MapMirrorRow::at<L, 16>(q, seq, j);
-            const float2 c = cmul(t1[j % T1N], t2[j / T1N]);
+            const float2 c = cmul(t1[buf][j % T1N], t2[buf][j / T1N]);
             twiddle_powers<16, true>(&x[16 * q], tws[QB + q][t], c);
             dft<16, -1>(reinterpret_cast<float2(&)[16]>(x[16 * q]));
 #pragma unroll
-            for (int r = 0; r < 16; ++r) x[16 * q + r] = cmul(x[16 * q + r], rho[r]);
+            for (int r = 0; r < 16; ++r) x[16 * q + r] = cmul(x[16 * q + r], rho[buf][r]);
         }
         float4* row4 = reinterpret_cast<float4*>(Y + ((size_t)m1 << LOGL));
         if (t != 0) {
@@ -437,6 +445,8 @@ __global__ void __launch_bounds__(256, 2)
         }
         wait_tile();
         __syncthreads();  // tile copies visible; previous tile done with the tables
+        // The tile's column tables are first read by the last inverse stage, several block barriers
+        // later: no barrier of their own, so the few threads computing them overlap the first stages.
         if (!SEED) {
             for (int i = t; i < CPT * (RL + U1N + U2N); i += NT) {
                 int c, kind, r;
@@ -452,7 +462,6 @@ __global__ void __launch_bounds__(256, 2)
                 else u2[c * U2N + r] = w;
             }
         }
-        __syncthreads();
         float2 x[E];
         if (TMA) {  // row-major tile: element m1 of column c at sm[m1 * CPT + c]
 #pragma unroll
