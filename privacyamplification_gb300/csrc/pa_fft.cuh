@@ -142,12 +142,18 @@ __device__ __forceinline__ void stage_bases(float2* w) {
     }
 }
 
+struct NoHook {
+    __device__ __forceinline__ void operator()() const {}
+};
+
 // Exchange between stage A (radix RA, NSA, map MA: its outputs) and stage B (radix RB, map MB: its
 // inputs) through the shared tile sm (sequence stride SP, padding shift S).  Starts with a barrier
-// so that earlier reads of sm are complete.
-template <int L, int SP, int S, int E, int RA, int NSA, class MA, int RB, class MB>
-__device__ __forceinline__ void exchange(float2 (&x)[E], float2* sm) {
+// so that earlier reads of sm are complete; `after_barrier` runs right after it (a copy into memory
+// that every thread has finished reading can start there without a barrier of its own).
+template <int L, int SP, int S, int E, int RA, int NSA, class MA, int RB, class MB, class Hook = NoHook>
+__device__ __forceinline__ void exchange(float2 (&x)[E], float2* sm, Hook after_barrier = Hook()) {
     __syncthreads();
+    after_barrier();
 #pragma unroll
     for (int q = 0; q < E / RA; ++q) {
         int seq, j;

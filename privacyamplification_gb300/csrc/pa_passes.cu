@@ -328,7 +328,7 @@ __device__ __forceinline__ int spec_index(int c, int k1) {
 template <int LOGL, bool SEED>
 __global__ void __launch_bounds__(256, 2)
     k_pass_b(const __grid_constant__ CUtensorMap mapY, const float2* __restrict__ Y, float2* __restrict__ Z,
-             BlockGeom g, float2* __restrict__ spec, int* err) {
+             BlockGeom g, float2* __restrict__ spec, int* err, int early) {
     constexpr int L = 1 << LOGL, NT = 256, E = 32, CPT = 8192 / L, LR = L / 16, SP = TileStride<L>::value;
     constexpr bool TMA = CPT <= 128;              // box inner extent 2*CPT floats <= 256
     constexpr int BOXR = L < 256 ? L : 256;       // rows per box
@@ -342,14 +342,26 @@ __global__ void __launch_bounds__(256, 2)
     // keeping per-column tables, which would not fit in shared memory.
     constexpr bool LEAN = LOGL <= 6;
     constexpr int U1N = LEAN ? 0 : (NSL < 16 ? NSL : 16), U2N = LEAN ? 0 : NSL / U1N;  // W_N^{j k2}
+    // The last inverse stage writes straight from registers when the linear map gives each thread both
+    // columns of a pair for the same rows; the tile buffer is then free during that stage and the next
+    // tile's copies overlap with it.
+    constexpr bool DIRECT = CPT == 2 && NSL == NT && QL == 2;
+    constexpr int NBOX = L / BOXR;               // TMA boxes per tile
+    // Shared memory: [tile boxes 0 .. early-1][tile / exchange buffer][tables].  A tile occupies the
+    // first `early` boxes' own space and the start of the exchange buffer, so (key pass, DIRECT) the
+    // next tile's first boxes are copied as soon as the current tile is in registers, the rest after
+    // the last exchange.
+    if (!(TMA && DIRECT && !SEED)) early = 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float2* sm = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    float2* srow = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    float2* sm = srow + early * BOXR * CPT;
     float2* sigma = sm + CPT * SP;       // [CPT][RL]   conj(W_N^{NSL r k2})
     float2* u1 = sigma + CPT * RL;       // [CPT][U1N]  W_N^{k2 (j % 16)}
     float2* u2 = u1 + CPT * U1N;         // [CPT][U2N]  W_N^{k2 16 (j / 16)}
     float2* tws = u2 + CPT * U2N;        // [QB | 2 | QB | QL (unless LEAN)][NT] per-thread stage bases
     constexpr int U1D = U1N > 0 ? U1N : 1, U2D = U2N > 0 ? U2N : 1;  // divisors (unused when LEAN)
-    __shared__ __align__(8) uint64_t bar;       // TMA completion of the current tile
+    __shared__ __align__(8) uint64_t bar;       // TMA completion of the current tile (boxes early ..)
+    __shared__ __align__(8) uint64_t bar_early; // TMA completion of boxes 0 .. early-1
     __shared__ __align__(8) uint64_t bar_spec;  // bulk copy of the tile's seed spectrum (key pass)
     __shared__ int s_fail;                      // a bounded wait expired: stop waiting
     const uint32_t n2 = 1u << g.log_n2;
@@ -388,15 +400,17 @@ __global__ void __launch_bounds__(256, 2)
     // (caller: all threads past their last generic access to sm and a proxy fence).  Otherwise 8-byte
     // asynchronous copies into the padded column layout sm[c * SP + pad(m1)].  The row segments of
     // neighbouring tiles share sectors, so both forms read through L2 normally.
+    auto load_boxes = [&](int tl, int b0, int b1, uint64_t* bb) {  // TMA boxes [b0, b1) of tile tl
+        if (tl >= ntiles || b0 >= b1 || t != 0) return;
+        mbar_expect_tx(bb, (uint32_t)((b1 - b0) * BOXR * CPT * sizeof(float2)));
+#pragma unroll 1
+        for (int b = b0; b < b1; ++b) tma_load_2d(srow + b * BOXR * CPT, &mapY, 2 * CPT * tl, BOXR * b, bb);
+    };
     auto load_tile = [&](int tl) {
         if (tl >= ntiles) return;
         if (TMA) {
-            if (t == 0) {
-                mbar_expect_tx(&bar, (uint32_t)(CPT * L * sizeof(float2)));
-#pragma unroll 1
-                for (int b = 0; b < L / BOXR; ++b)
-                    tma_load_2d(sm + b * BOXR * CPT, &mapY, 2 * CPT * tl, BOXR * b, &bar);
-            }
+            load_boxes(tl, 0, early, &bar_early);
+            load_boxes(tl, early, NBOX, &bar);
         } else {
 #pragma unroll 4
             for (int i = 0; i < L * CPT / 2 / NT; ++i) {
@@ -407,14 +421,18 @@ __global__ void __launch_bounds__(256, 2)
             }
         }
     };
-    uint32_t parity = 0;
+    uint32_t parity = 0, parity_early = 0;
+    auto wait_bar = [&](uint64_t* bb, uint32_t& par) {
+        if (!s_fail && !mbar_wait(bb, par)) {
+            s_fail = 1;
+            atomicExch(err, kErrTmaTimeout);
+        }
+        par ^= 1u;
+    };
     auto wait_tile = [&]() {
         if (TMA) {
-            if (!s_fail && !mbar_wait(&bar, parity)) {
-                s_fail = 1;
-                atomicExch(err, kErrTmaTimeout);
-            }
-            parity ^= 1u;
+            if (early > 0) wait_bar(&bar_early, parity_early);
+            if (early < NBOX) wait_bar(&bar, parity);
         } else {
             cp_async_wait_all();
         }
@@ -422,14 +440,11 @@ __global__ void __launch_bounds__(256, 2)
     if (t == 0) {
         s_fail = 0;
         mbar_init(&bar, 1);
+        mbar_init(&bar_early, 1);
         mbar_init(&bar_spec, 1);
     }
     __syncthreads();
     uint32_t parity_spec = 0;
-    // The last inverse stage writes straight from registers when the linear map gives each thread both
-    // columns of a pair for the same rows; the tile buffer is then free during that stage and the next
-    // tile's copies overlap with it.
-    constexpr bool DIRECT = CPT == 2 && NSL == NT && QL == 2;
     fence_proxy_async();
     load_tile(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -469,21 +484,29 @@ __global__ void __launch_bounds__(256, 2)
                 int seq, j;
                 Lin::at<L, P::RA>(q, seq, j);
 #pragma unroll
-                for (int r = 0; r < P::RA; ++r) x[q * P::RA + r] = sm[(j + r * (L / P::RA)) * CPT + seq];
+                for (int r = 0; r < P::RA; ++r) x[q * P::RA + r] = srow[(j + r * (L / P::RA)) * CPT + seq];
             }
         } else {
             gather_inputs<L, SP, E, P::RA, Lin>(x, sm);
         }
         stage<P::RA, 1, -1, E>(x, nullptr);
+        // after the first exchange's barrier every thread has read the tile: the next tile's own boxes
+        // are copied under the rest of this tile's work
+        auto copy_early = [&]() {
+            if (early > 0) {
+                fence_proxy_async();
+                load_boxes(tile + (int)gridDim.x, 0, early, &bar_early);
+            }
+        };
         if (P::NSTAGE == 2) {
-            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm);
+            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm, copy_early);
             float2 w[QB > 0 ? QB : 1];
 #pragma unroll
             for (int q = 0; q < QB; ++q) w[q] = tws[q * NT + t];
             stage<P::RB, P::RA, -1, E>(x, w);
             exchange<L, SP, 4, E, P::RB, P::RA, Lin, 16, MapMirrorPair>(x, sm);
         } else {
-            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorPair>(x, sm);
+            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorPair>(x, sm, copy_early);
         }
         float2* tspec = spec + (size_t)tile * (CPT * L);
         const bool special = tile == 0;  // pair 0 holds the self-mirrored columns 0 and N2/2
@@ -634,10 +657,11 @@ __global__ void __launch_bounds__(256, 2)
         } else {
             exchange<L, SP, 4, E, 16, 1, MapMirrorPair, RL, Lin>(x, sm);
         }
-        if (DIRECT) {  // after the last exchange sm is free until the next tile
+        if (DIRECT) {  // after the last exchange sm is free until the next tile: the rest of its boxes
             __syncthreads();
             fence_proxy_async();
-            load_tile(tile + gridDim.x);
+            if (TMA) load_boxes(tile + (int)gridDim.x, early, NBOX, &bar);
+            else load_tile(tile + gridDim.x);
         }
 #pragma unroll
         for (int q = 0; q < QL; ++q) {
@@ -817,22 +841,25 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
                 x[16 + 15 - r] = make_float2(b.z, b.w);
             }
         }
-        if (early > 0) {  // the row's own boxes are read: gather the next row's under this row's transform
-            __syncthreads();
-            fence_proxy_async();
-            load_early(m1 + gridDim.x);
-        }
         stage<16, 1, +1, E>(x, nullptr);
+        // after the first exchange's barrier every thread has read the row: the next row's own boxes
+        // are gathered under the rest of this row's transform
+        auto gather_early = [&]() {
+            if (early > 0) {
+                fence_proxy_async();
+                load_early(m1 + gridDim.x);
+            }
+        };
         {
             float2 w[4];
             if (P::NSTAGE == 2) {
-                exchange<L, SP, 4, E, 16, 1, MapMirrorRow, P::RB, Lin>(x, sm);
+                exchange<L, SP, 4, E, 16, 1, MapMirrorRow, P::RB, Lin>(x, sm, gather_early);
 #pragma unroll
                 for (int q = 0; q < QB; ++q) w[q] = tws[q][t];
                 stage_tab<P::RB, 16, +1, E, L, Lin>(x, tab2);
                 exchange<L, SP, 4, E, P::RB, 16, Lin, RL, Lin>(x, sm);
             } else {
-                exchange<L, SP, 4, E, 16, 1, MapMirrorRow, RL, Lin>(x, sm);
+                exchange<L, SP, 4, E, 16, 1, MapMirrorRow, RL, Lin>(x, sm, gather_early);
             }
             // the exchange buffer is free: the rest of the next row's copy runs under the last stage
             __syncthreads();
@@ -1010,14 +1037,34 @@ static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2*
     constexpr size_t words = (size_t)CPT * TileStride<L>::value + (size_t)CPT * (RL + U1N + U2N) +
                              (size_t)(2 * QB + 2 + QL) * 256;
     static_assert(words * sizeof(float2) + 128 <= 112 * 1024, "pass B tile too large for two CTAs per SM");
-    size_t smem = words * sizeof(float2) + 128;  // + alignment of the TMA destination
+    const size_t smem = words * sizeof(float2) + 128;  // + alignment of the TMA destination
     int grid = grid_units((1u << g.log_n2) / CPT, 2 * num_sms);
     if (seed) {
         smem_attr(k_pass_b<LOGL, true>, smem);
-        k_pass_b<LOGL, true><<<grid, 256, smem, s>>>(maps.y, Y, Z, g, spec, err);
+        k_pass_b<LOGL, true><<<grid, 256, smem, s>>>(maps.y, Y, Z, g, spec, err, 0);
     } else {
-        smem_attr(k_pass_b<LOGL, false>, smem);
-        k_pass_b<LOGL, false><<<grid, 256, smem, s>>>(maps.y, Y, Z, g, spec, err);
+        // key pass: as many of the next tile's boxes as fit beside the tile while two CTAs stay resident
+        static const int early = [] {
+            constexpr int BOXR = L < 256 ? L : 256;
+            constexpr bool direct = CPT == 2 && NSL == 256 && 32 / RL == 2 && CPT <= 128;
+            const size_t box = (size_t)BOXR * CPT * sizeof(float2);
+            int e = direct ? L / BOXR : 0;
+            for (; e > 0; --e) {
+                int per_sm = 0;
+                const size_t bytes = smem + (size_t)e * box;
+                if (cudaFuncSetAttribute(k_pass_b<LOGL, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes) == cudaSuccess &&
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass_b<LOGL, false>, 256, bytes) ==
+                        cudaSuccess &&
+                    per_sm >= 2)
+                    break;
+            }
+            cudaGetLastError();  // a refused attribute above is not an error of this launch
+            return e;
+        }();
+        const size_t bytes = smem + (size_t)early * (size_t)(L < 256 ? L : 256) * CPT * sizeof(float2);
+        smem_attr(k_pass_b<LOGL, false>, bytes);
+        k_pass_b<LOGL, false><<<grid, 256, bytes, s>>>(maps.y, Y, Z, g, spec, err, early);
     }
     return (int)cudaGetLastError();
 }
