@@ -240,10 +240,12 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     row_tables(blockIdx.x, 0);
     int buf = 0;
     for (uint32_t m1 = blockIdx.x; m1 < n1; m1 += gridDim.x, buf ^= 1) {
-        __syncthreads();  // previous row done with bits[buf ^ 1] / tables [buf ^ 1] / sm
+        cp_async_wait_group<0>();  // this thread's copy of row m1 (the only one in flight) has landed
+        // One barrier: row m1's bits and tables visible; the previous row is past its mirror stage, the
+        // last reader of tables[buf ^ 1] (bits[buf ^ 1] were read at its start).
+        __syncthreads();
         fetch_row(m1 + gridDim.x, buf ^ 1);
-        cp_async_wait_group<1>();  // this thread's copy of row m1 has landed
-        __syncthreads();  // all copies of row m1 visible
+        row_tables(m1 + gridDim.x, buf ^ 1);
         ones += __popc(bits[buf][2 * t]) + __popc(bits[buf][2 * t + 1]);
         float2 x[E];
 #pragma unroll
@@ -257,7 +259,6 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
                 x[q * P::RA + r] = make_float2((float)((w >> (sh + 1)) & 1u), (float)((w >> sh) & 1u));
             }
         }
-        row_tables(m1 + gridDim.x, buf ^ 1);
         stage<P::RA, 1, -1, E>(x, nullptr);
         if (P::NSTAGE == 2) {
             exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm);
