@@ -321,6 +321,28 @@ __device__ __forceinline__ int spec_index(int c, int k1) {
     return (c * 16 + r) * LR + jj;
 }
 
+// Slots of pass B's per-thread stage-base table (NT = 256 entries each): forward second stage, mirror
+// stage (2), inverse second stage, last inverse stage.  When the linear map gives a thread the same
+// butterfly index j in both of its butterflies (NT a multiple of L/R) one slot serves both, and with
+// first-stage radix 16 the inverse second stage's bases are the conjugates of the forward ones.
+template <int LOGL>
+struct PassBBases {
+    static constexpr int L = 1 << LOGL, NT = 256, E = 32;
+    using P = Plan<LOGL>;
+    static constexpr int RL = P::RA, NSL = L / RL, QB = P::NSTAGE == 2 ? E / P::RB : 0, QL = E / RL;
+    static constexpr bool LEAN = LOGL <= 6;
+    static constexpr bool SHARE2 = P::NSTAGE == 2 && P::RA == 16 && NT % (L / P::RB) == 0;
+    static constexpr bool SHAREL = !LEAN && NT % NSL == 0;
+    static constexpr int F2 = 0, NF2 = SHARE2 ? 1 : QB;
+    static constexpr int M = F2 + NF2;
+    static constexpr int I2 = M + 2, NI2 = SHARE2 ? 0 : QB;
+    static constexpr int LS = I2 + NI2, NLS = LEAN ? 0 : (SHAREL ? 1 : QL);
+    static constexpr int SLOTS = LS + NLS;
+    static constexpr int f2(int q) { return F2 + (SHARE2 ? 0 : q); }
+    static constexpr int i2(int q) { return I2 + q; }
+    static constexpr int ls(int q) { return LS + (SHAREL ? 0 : q); }
+};
+
 // 256 threads x 32 values: a tile is 8192 complex values (one mirror pair of 4096-point columns at
 // n = 2^27), so that two CTAs share an SM and hide each other's HBM latency.
 // Input: Y (row-major pairs, as pass A wrote it) through 2D TMA boxes of 256 rows x CPT columns, or
@@ -359,7 +381,8 @@ __global__ void __launch_bounds__(256, 2)
     float2* sigma = sm + CPT * SP;       // [CPT][RL]   conj(W_N^{NSL r k2})
     float2* u1 = sigma + CPT * RL;       // [CPT][U1N]  W_N^{k2 (j % 16)}
     float2* u2 = u1 + CPT * U1N;         // [CPT][U2N]  W_N^{k2 16 (j / 16)}
-    float2* tws = u2 + CPT * U2N;        // [QB | 2 | QB | QL (unless LEAN)][NT] per-thread stage bases
+    float2* tws = u2 + CPT * U2N;        // [PassBBases slots][NT] per-thread stage bases
+    using TB = PassBBases<LOGL>;
     constexpr int U1D = U1N > 0 ? U1N : 1, U2D = U2N > 0 ? U2N : 1;  // divisors (unused when LEAN)
     __shared__ __align__(8) uint64_t bar;       // TMA completion of the current tile (boxes early ..)
     __shared__ __align__(8) uint64_t bar_early; // TMA completion of boxes 0 .. early-1
@@ -375,25 +398,25 @@ __global__ void __launch_bounds__(256, 2)
         if (P::NSTAGE == 2) {
             stage_bases<L, P::RB, P::RA, -1, E, Lin>(w);
 #pragma unroll
-            for (int q = 0; q < QB; ++q) tws[q * NT + t] = w[q];
+            for (int q = 0; q < TB::NF2; ++q) tws[TB::f2(q) * NT + t] = w[q];
         }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             int seq, j;
             MapMirrorPair::at<L, 16>(q, seq, j);
-            tws[(QB + q) * NT + t] = unit_root<-1>(j, L);
+            tws[(TB::M + q) * NT + t] = unit_root<-1>(j, L);
         }
-        if (P::NSTAGE == 2) {
+        if (P::NSTAGE == 2 && !TB::SHARE2) {
             stage_bases<L, P::RB, 16, +1, E, Lin>(w);
 #pragma unroll
-            for (int q = 0; q < QB; ++q) tws[(QB + 2 + q) * NT + t] = w[q];
+            for (int q = 0; q < TB::NI2; ++q) tws[TB::i2(q) * NT + t] = w[q];
         }
         if (!LEAN) {
 #pragma unroll
-            for (int q = 0; q < QL; ++q) {
+            for (int q = 0; q < TB::NLS; ++q) {
                 int seq, j;
                 Lin::at<L, RL>(q, seq, j);
-                tws[(2 * QB + 2 + q) * NT + t] = unit_root<+1>(j % NSL, NSL * RL);
+                tws[TB::ls(q) * NT + t] = unit_root<+1>(j % NSL, NSL * RL);
             }
         }
     }
@@ -503,7 +526,7 @@ __global__ void __launch_bounds__(256, 2)
             exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm, copy_early);
             float2 w[QB > 0 ? QB : 1];
 #pragma unroll
-            for (int q = 0; q < QB; ++q) w[q] = tws[q * NT + t];
+            for (int q = 0; q < QB; ++q) w[q] = tws[TB::f2(q) * NT + t];
             stage<P::RB, P::RA, -1, E>(x, w);
             exchange<L, SP, 4, E, P::RB, P::RA, Lin, 16, MapMirrorPair>(x, sm);
         } else {
@@ -528,7 +551,7 @@ __global__ void __launch_bounds__(256, 2)
             }
         }
         {
-            float2 w[2] = {tws[QB * NT + t], tws[(QB + 1) * NT + t]};
+            float2 w[2] = {tws[TB::M * NT + t], tws[(TB::M + 1) * NT + t]};
             stage<16, LR, -1, E>(x, w);
         }
         if (spec_smem) {
@@ -652,7 +675,8 @@ __global__ void __launch_bounds__(256, 2)
             exchange<L, SP, 4, E, 16, 1, MapMirrorPair, P::RB, Lin>(x, sm);
             float2 w[QB > 0 ? QB : 1];
 #pragma unroll
-            for (int q = 0; q < QB; ++q) w[q] = tws[(QB + 2 + q) * NT + t];
+            for (int q = 0; q < QB; ++q)
+                w[q] = TB::SHARE2 ? cconj(tws[TB::f2(q) * NT + t]) : tws[TB::i2(q) * NT + t];
             stage<P::RB, 16, +1, E>(x, w);
             exchange<L, SP, 4, E, P::RB, 16, Lin, RL, Lin>(x, sm);
         } else {
@@ -675,7 +699,7 @@ __global__ void __launch_bounds__(256, 2)
                 wbase = unit_root<+1>(j % NSL, NSL * RL);
             } else {
                 c = cconj(cmul(u1[seq * U1N + j % U1D], u2[seq * U2N + j / U1D]));
-                wbase = tws[(2 * QB + 2 + q) * NT + t];
+                wbase = tws[TB::ls(q) * NT + t];
             }
             twiddle_powers<RL, true>(&x[q * RL], wbase, c);
             dft<RL, +1>(reinterpret_cast<float2(&)[RL]>(x[q * RL]));
@@ -1034,9 +1058,8 @@ static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2*
     constexpr int L = 1 << LOGL, CPT = 8192 / L, RL = Plan<LOGL>::RA, NSL = L / RL;
     constexpr bool LEAN = LOGL <= 6;
     constexpr int U1N = LEAN ? 0 : (NSL < 16 ? NSL : 16), U2N = LEAN ? 0 : NSL / U1N;
-    constexpr int QB = Plan<LOGL>::NSTAGE == 2 ? 32 / Plan<LOGL>::RB : 0, QL = LEAN ? 0 : 32 / RL;
     constexpr size_t words = (size_t)CPT * TileStride<L>::value + (size_t)CPT * (RL + U1N + U2N) +
-                             (size_t)(2 * QB + 2 + QL) * 256;
+                             (size_t)PassBBases<LOGL>::SLOTS * 256;
     static_assert(words * sizeof(float2) + 128 <= 112 * 1024, "pass B tile too large for two CTAs per SM");
     const size_t smem = words * sizeof(float2) + 128;  // + alignment of the TMA destination
     int grid = grid_units((1u << g.log_n2) / CPT, 2 * num_sms);
