@@ -753,7 +753,7 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     constexpr int QB = P::NSTAGE == 2 ? E / P::RB : 0;
     constexpr int QL = E / RL;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ float2 tws[(QB > 0 ? QB : 1) + QL][NT];
+    __shared__ float2 tws[QL][NT];  // last-stage per-thread twiddle bases (the second stage reads tab2)
     __shared__ float2 tab2[P::NSTAGE == 2 ? P::RB * 16 : 1];  // second-stage twiddles
     __shared__ float redf[32];
     __shared__ __align__(8) uint64_t bar, bar_late;  // TMA completion: boxes [0, early), [early, nb)
@@ -771,16 +771,10 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     const int t = threadIdx.x, lane = t & 31;
     {
         float2 w[4];
-        if (P::NSTAGE == 2) {
-            stage_bases<L, P::RB, 16, +1, E, Lin>(w);
+        if (P::NSTAGE == 2) stage_bases<L, RL, 16 * P::RB, +1, E, Lin>(w);
+        else stage_bases<L, RL, 16, +1, E, Lin>(w);
 #pragma unroll
-            for (int q = 0; q < QB; ++q) tws[q][t] = w[q];
-            stage_bases<L, RL, 16 * P::RB, +1, E, Lin>(w);
-        } else {
-            stage_bases<L, RL, 16, +1, E, Lin>(w);
-        }
-#pragma unroll
-        for (int q = 0; q < QL; ++q) tws[(QB > 0 ? QB : 1) + q][t] = w[q];
+        for (int q = 0; q < QL; ++q) tws[q][t] = w[q];
         if (P::NSTAGE == 2) fill_stage_table<P::RB, 16, +1>(tab2);
     }
     float corr;
@@ -879,8 +873,6 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
             float2 w[4];
             if (P::NSTAGE == 2) {
                 exchange<L, SP, 4, E, 16, 1, MapMirrorRow, P::RB, Lin>(x, sm, gather_early);
-#pragma unroll
-                for (int q = 0; q < QB; ++q) w[q] = tws[q][t];
                 stage_tab<P::RB, 16, +1, E, L, Lin>(x, tab2);
                 exchange<L, SP, 4, E, P::RB, 16, Lin, RL, Lin>(x, sm);
             } else {
@@ -891,7 +883,7 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
             fence_proxy_async();
             load_late(m1 + gridDim.x);
 #pragma unroll
-            for (int q = 0; q < QL; ++q) w[q] = tws[(QB > 0 ? QB : 1) + q][t];
+            for (int q = 0; q < QL; ++q) w[q] = tws[q][t];
             stage<RL, (P::NSTAGE == 2 ? 16 * P::RB : 16), +1, E>(x, w);
         }
         // outputs: butterfly u = t + q*NT (j = u), sample m2 = j + NSL*r; lanes hold consecutive m2.
