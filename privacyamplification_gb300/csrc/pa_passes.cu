@@ -424,11 +424,17 @@ __global__ void __launch_bounds__(256, 2)
     // (caller: all threads past their last generic access to sm and a proxy fence).  Otherwise 8-byte
     // asynchronous copies into the padded column layout sm[c * SP + pad(m1)].  The row segments of
     // neighbouring tiles share sectors, so both forms read through L2 normally.
-    auto load_boxes = [&](int tl, int b0, int b1, uint64_t* bb) {  // TMA boxes [b0, b1) of tile tl
-        if (tl >= ntiles || b0 >= b1 || t != 0) return;
-        mbar_expect_tx(bb, (uint32_t)((b1 - b0) * BOXR * CPT * sizeof(float2)));
+    // TMA boxes [b0, b1) of tile tl, called by every thread: thread 0 announces the bytes, lane 0 of
+    // each warp issues every (NT/32)-th box (a copy landing first cannot complete the phase: its
+    // arrival is pending).
+    auto load_boxes = [&](int tl, int b0, int b1, uint64_t* bb) {
+        if (tl >= ntiles || b0 >= b1) return;
+        if (t == 0) mbar_expect_tx(bb, (uint32_t)((b1 - b0) * BOXR * CPT * sizeof(float2)));
+        if ((t & 31) == 0) {
 #pragma unroll 1
-        for (int b = b0; b < b1; ++b) tma_load_2d(srow + b * BOXR * CPT, &mapY, 2 * CPT * tl, BOXR * b, bb);
+            for (int b = b0 + (t >> 5); b < b1; b += NT / 32)
+                tma_load_2d(srow + b * BOXR * CPT, &mapY, 2 * CPT * tl, BOXR * b, bb);
+        }
     };
     auto load_tile = [&](int tl) {
         if (tl >= ntiles) return;
@@ -541,11 +547,11 @@ __global__ void __launch_bounds__(256, 2)
         if (spec_smem) {
             __syncthreads();  // every thread done reading sm
             fence_proxy_async();
-            if (t == 0) {
-                constexpr uint32_t kBytes = CPT * L * sizeof(float2), kChunk = 16384;
-                mbar_expect_tx(&bar_spec, kBytes);
+            constexpr uint32_t kBytes = CPT * L * sizeof(float2), kChunk = 16384;
+            if (t == 0) mbar_expect_tx(&bar_spec, kBytes);
+            if ((t & 31) == 0) {  // one chunk per warp
 #pragma unroll 1
-                for (uint32_t off = 0; off < kBytes; off += kChunk)
+                for (uint32_t off = (uint32_t)(t >> 5) * kChunk; off < kBytes; off += (NT / 32) * kChunk)
                     bulk_load(reinterpret_cast<char*>(sm) + off, reinterpret_cast<const char*>(tspec) + off, kChunk,
                               &bar_spec);
             }
@@ -786,20 +792,25 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     // rows holding at least one output sample: m1 < min(N1, ceil(out_bits / 2))
     const uint32_t rows_out = (uint32_t)(((uint64_t)g.out_bits + 1ull) / 2ull < n1 ? (g.out_bits + 1u) / 2u : n1);
     const uint32_t box_bytes = (uint32_t)(boxt * cpt * sizeof(float2));
-    auto load_early = [&](uint32_t r) {  // boxes [0, early) of row r (TMA only)
-        if (r >= rows_out || early == 0 || t != 0) return;
-        mbar_expect_tx(&bar, (uint32_t)early * box_bytes);
+    // Boxes [b0, b1) of row r, called by every thread: thread 0 announces the bytes, and lane 0 of
+    // each warp issues every (NT/32)-th box, so no single warp is held up issuing a row's copies.
+    // A copy that lands before the announcement cannot complete the phase: its arrival is pending.
+    auto issue_boxes = [&](uint32_t r, int b0, int b1, uint64_t* bb) {
+        if (r >= rows_out || b0 >= b1) return;
+        if (t == 0) mbar_expect_tx(bb, (uint32_t)(b1 - b0) * box_bytes);
+        if (lane == 0) {
 #pragma unroll 1
-        for (int b = 0; b < early; ++b) tma_load_3d(srow + (size_t)b * boxt * cpt, &mapZ, 0, (int)r, boxt * b, &bar);
+            for (int b = b0 + (t >> 5); b < b1; b += NT / 32)
+                tma_load_3d(srow + (size_t)b * boxt * cpt, &mapZ, 0, (int)r, boxt * b, bb);
+        }
+    };
+    auto load_early = [&](uint32_t r) {  // boxes [0, early) of row r (TMA only)
+        if (early > 0) issue_boxes(r, 0, early, &bar);
     };
     auto load_late = [&](uint32_t r) {  // boxes [early, nb) of row r, or the whole row by cooperative loads
         if (r >= rows_out) return;
         if (tma) {
-            if (early == nb || t != 0) return;
-            mbar_expect_tx(&bar_late, (uint32_t)(nb - early) * box_bytes);
-#pragma unroll 1
-            for (int b = early; b < nb; ++b)
-                tma_load_3d(srow + (size_t)b * boxt * cpt, &mapZ, 0, (int)r, boxt * b, &bar_late);
+            issue_boxes(r, early, nb, &bar_late);
         } else {
             const float4* z4 = reinterpret_cast<const float4*>(Z);
             float4* s4 = reinterpret_cast<float4*>(srow);
