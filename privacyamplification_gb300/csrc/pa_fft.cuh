@@ -148,11 +148,13 @@ struct NoHook {
 
 // Exchange between stage A (radix RA, NSA, map MA: its outputs) and stage B (radix RB, map MB: its
 // inputs) through the shared tile sm (sequence stride SP, padding shift S).  Starts with a barrier
-// so that earlier reads of sm are complete; `after_barrier` runs right after it (a copy into memory
-// that every thread has finished reading can start there without a barrier of its own).
-template <int L, int SP, int S, int E, int RA, int NSA, class MA, int RB, class MB, class Hook = NoHook>
+// so that earlier reads of sm are complete (LEAD = false: the caller's last barrier already follows
+// them); `after_barrier` runs right after it (a copy into memory that every thread has finished
+// reading can start there without a barrier of its own).
+template <int L, int SP, int S, int E, int RA, int NSA, class MA, int RB, class MB, class Hook = NoHook,
+          bool LEAD = true>
 __device__ __forceinline__ void exchange(float2 (&x)[E], float2* sm, Hook after_barrier = Hook()) {
-    __syncthreads();
+    if (LEAD) __syncthreads();
     after_barrier();
 #pragma unroll
     for (int q = 0; q < E / RA; ++q) {

@@ -260,15 +260,17 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
             }
         }
         stage<P::RA, 1, -1, E>(x, nullptr);
+        // the first exchange needs no leading barrier: the row's barrier above follows the previous
+        // row's last reads of sm, and nothing reads sm since
         if (P::NSTAGE == 2) {
-            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm);
+            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin, NoHook, false>(x, sm);
             float2 w[QB > 0 ? QB : 1];
 #pragma unroll
             for (int q = 0; q < QB; ++q) w[q] = tws[q][t];
             stage<P::RB, P::RA, -1, E>(x, w);
             exchange<L, SP, 4, E, P::RB, P::RA, Lin, 16, MapMirrorRow>(x, sm);
         } else {
-            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorRow>(x, sm);
+            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorRow, NoHook, false>(x, sm);
         }
         // mirror stage (NS = L/16) with the 4-step twiddle W_N^{m1 (j + LR r)} folded in:
         // W_N^{m1 j} on the inputs, rho[r] = W_N^{m1 LR r} on the outputs.
