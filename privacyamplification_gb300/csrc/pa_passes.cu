@@ -765,6 +765,11 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     __shared__ float2 tab2[P::NSTAGE == 2 ? P::RB * 16 : 1];  // second-stage twiddles
     __shared__ float redf[32];
     __shared__ __align__(8) uint64_t bar, bar_late;  // TMA completion: boxes [0, early), [early, nb)
+    // Parity words of a row (the KR * NSL / 32 live words of each plane), double-buffered by row: lane 0
+    // of each warp writes its ballots here, and every thread copies the previous row's words out with
+    // coalesced stores after the next row's first barrier.
+    constexpr int PW = KR * NSL / 32;
+    __shared__ uint32_t pstage[2][2][PW];
     __shared__ int s_fail;
     const uint32_t n1 = 1u << g.log_n1;
     const int cpt = 8192 >> g.log_n1;               // pass B tile width (columns)
@@ -844,14 +849,19 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     load_early(blockIdx.x);
     load_late(blockIdx.x);
     float res = 0.f;
-    for (uint32_t m1 = blockIdx.x; m1 < rows_out; m1 += gridDim.x) {
-        uint32_t* pe = planes + (size_t)m1 * (L / 32);
-        uint32_t* po = pe + plane_words;
+    auto flush = [&](uint32_t row, int b) {  // staged parity words of `row` (buffer b) to the planes
+        uint32_t* dst = planes + (size_t)row * (L / 32);
+        for (int i = t; i < 2 * PW; i += NT)
+            dst[(i >= PW ? plane_words : 0) + (size_t)(i % PW)] = pstage[b][i / PW][i % PW];
+    };
+    int pb = 0;
+    for (uint32_t m1 = blockIdx.x; m1 < rows_out; m1 += gridDim.x, pb ^= 1) {
         if (tma) {
             if (early > 0) wait_bar(&bar, parity);
             if (early < nb) wait_bar(&bar_late, parity_late);
         }
-        __syncthreads();  // row in shared memory
+        __syncthreads();  // row in shared memory; the previous row's parity words staged
+        if (m1 != blockIdx.x) flush(m1 - gridDim.x, pb ^ 1);
         float2 x[E];
         const float4* row4 = reinterpret_cast<const float4*>(srow);
         if (t != 0) {
@@ -919,12 +929,18 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
                 const uint32_t be = __ballot_sync(0xffffffffu, ok0 && ((int)r0 & 1));
                 const uint32_t bo = __ballot_sync(0xffffffffu, ok1 && ((int)r1 & 1));
                 if (lane == 0) {
-                    pe[m2 >> 5] = be;
-                    po[m2 >> 5] = bo;
+                    pstage[pb][0][m2 >> 5] = be;
+                    pstage[pb][1][m2 >> 5] = bo;
                 }
             }
         }
         if (!tma) __syncthreads();  // cooperative loads of the next row happen at the top
+    }
+    // the last row's parity words (the barrier orders them after every warp's ballots)
+    __syncthreads();
+    {
+        const uint32_t nrows = rows_out > blockIdx.x ? (rows_out - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+        if (nrows > 0) flush(blockIdx.x + (nrows - 1) * gridDim.x, (int)((nrows - 1) & 1));
     }
     float bm = block_max_f(res, redf);
     if (threadIdx.x == 0) atomicMax(resid_bits, __float_as_uint(bm));
