@@ -373,10 +373,10 @@ __global__ void __launch_bounds__(256, 2)
     constexpr bool DIRECT = CPT == 2 && NSL == NT && QL == 2;
     constexpr int NBOX = L / BOXR;               // TMA boxes per tile
     // Shared memory: [tile boxes 0 .. early-1][tile / exchange buffer][tables].  A tile occupies the
-    // first `early` boxes' own space and the start of the exchange buffer, so (key pass, DIRECT) the
-    // next tile's first boxes are copied as soon as the current tile is in registers, the rest after
-    // the last exchange.
-    if (!(TMA && DIRECT && !SEED)) early = 0;
+    // first `early` boxes' own space and the start of the exchange buffer, so the next tile's first
+    // boxes are copied as soon as the current tile is in registers, the rest once the exchange buffer
+    // is free (after the last exchange in the DIRECT key pass, else at the next tile's start).
+    if (!TMA) early = 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* srow = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     float2* sm = srow + early * BOXR * CPT;
@@ -487,7 +487,8 @@ __global__ void __launch_bounds__(256, 2)
             if (tile != (int)blockIdx.x) {
                 __syncthreads();  // previous tile done with sm
                 fence_proxy_async();
-                load_tile(tile);
+                if (TMA) load_boxes(tile, early, NBOX, &bar);  // its first boxes came early
+                else load_tile(tile);
             }
         }
         wait_tile();
@@ -1084,30 +1085,31 @@ static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2*
     static_assert(words * sizeof(float2) + 128 <= 112 * 1024, "pass B tile too large for two CTAs per SM");
     const size_t smem = words * sizeof(float2) + 128;  // + alignment of the TMA destination
     int grid = grid_units((1u << g.log_n2) / CPT, 2 * num_sms);
+    // As many of the next tile's boxes as fit beside the tile while two CTAs stay resident per SM.
+    constexpr int BOXR = L < 256 ? L : 256;
+    const size_t box = (size_t)BOXR * CPT * sizeof(float2);
+    auto early_boxes = [&](auto kernel) {
+        int e = CPT <= 128 ? L / BOXR : 0;
+        for (; e > 0; --e) {
+            int per_sm = 0;
+            const size_t bytes = smem + (size_t)e * box;
+            if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) ==
+                    cudaSuccess &&
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, bytes) == cudaSuccess &&
+                per_sm >= 2)
+                break;
+        }
+        cudaGetLastError();  // a refused attribute above is not an error of this launch
+        return e;
+    };
     if (seed) {
-        smem_attr(k_pass_b<LOGL, true>, smem);
-        k_pass_b<LOGL, true><<<grid, 256, smem, s>>>(maps.y, Y, Z, g, spec, err, 0);
+        static const int early = early_boxes(k_pass_b<LOGL, true>);
+        const size_t bytes = smem + (size_t)early * box;
+        smem_attr(k_pass_b<LOGL, true>, bytes);
+        k_pass_b<LOGL, true><<<grid, 256, bytes, s>>>(maps.y, Y, Z, g, spec, err, early);
     } else {
-        // key pass: as many of the next tile's boxes as fit beside the tile while two CTAs stay resident
-        static const int early = [] {
-            constexpr int BOXR = L < 256 ? L : 256;
-            constexpr bool direct = CPT == 2 && NSL == 256 && 32 / RL == 2 && CPT <= 128;
-            const size_t box = (size_t)BOXR * CPT * sizeof(float2);
-            int e = direct ? L / BOXR : 0;
-            for (; e > 0; --e) {
-                int per_sm = 0;
-                const size_t bytes = smem + (size_t)e * box;
-                if (cudaFuncSetAttribute(k_pass_b<LOGL, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)bytes) == cudaSuccess &&
-                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass_b<LOGL, false>, 256, bytes) ==
-                        cudaSuccess &&
-                    per_sm >= 2)
-                    break;
-            }
-            cudaGetLastError();  // a refused attribute above is not an error of this launch
-            return e;
-        }();
-        const size_t bytes = smem + (size_t)early * (size_t)(L < 256 ? L : 256) * CPT * sizeof(float2);
+        static const int early = early_boxes(k_pass_b<LOGL, false>);
+        const size_t bytes = smem + (size_t)early * box;
         smem_attr(k_pass_b<LOGL, false>, bytes);
         k_pass_b<LOGL, false><<<grid, 256, bytes, s>>>(maps.y, Y, Z, g, spec, err, early);
     }
