@@ -347,9 +347,11 @@ struct PassBBases {
 
 // 256 threads x 32 values: a tile is 8192 complex values (one mirror pair of 4096-point columns at
 // n = 2^27), so that two CTAs share an SM and hide each other's HBM latency.
-// Input: Y (row-major pairs, as pass A wrote it) through 2D TMA boxes of 256 rows x CPT columns, or
-// per-thread asynchronous copies when the tile is too wide for a box.  Output (key pass): Z, tile-major
-// (Z[tile][m1][CPT columns]), stored coalesced from registers; (seed pass): spec.
+// Input: Y (row-major pairs, as pass A wrote it) through 2D TMA boxes of 256 rows x CPT columns (the
+// next tile's first `early` boxes copied into a buffer of their own as soon as the current tile is in
+// registers; every warp issues its share), or per-thread asynchronous copies when the tile is too wide
+// for a box.  Output (key pass): Z, tile-major (Z[tile][m1][CPT columns]), stored coalesced from
+// registers; (seed pass): spec.
 template <int LOGL, bool SEED>
 __global__ void __launch_bounds__(256, 2)
     k_pass_b(const __grid_constant__ CUtensorMap mapY, const float2* __restrict__ Y, float2* __restrict__ Z,
@@ -741,9 +743,11 @@ __global__ void __launch_bounds__(256, 2)
 // or cooperative loads when a tile row is too wide for a box.  Shared memory holds [row boxes 0 ..
 // early-1][exchange buffer], so a row occupies the first `early` boxes' own space and the start of the
 // exchange buffer.  The next row's first `early` boxes are gathered as soon as the current row has been
-// read into registers (under the whole row's transform); the rest as soon as the last exchange has
-// finished with the buffer.  `early` is as many boxes as shared memory holds (all of them for rows up to
-// 2^13; 19 of 32 for rows of 2^14).
+// read into registers (issued after the first exchange's barrier, so they land under the rest of the
+// row's transform); the rest as soon as the last exchange has finished with the buffer.  `early` is as
+// many boxes as shared memory holds (all of them for rows up to 2^13; 19 of 32 for rows of 2^14 with
+// v = 3n/8).  Every warp issues its share of the boxes.  The parity words of a row are staged in
+// shared memory and written out with coalesced stores at the next row's start.
 // KEEP8: the last stage's outputs r < KEEP8 * RL / 8 (samples m2 = j + NSL r) are the only ones that can
 // fall below out_bits; the others are neither rounded nor stored, and the compiler drops their share of
 // the last radix stage.  Their plane words keep whatever the buffer held: k_finish never reads a word
