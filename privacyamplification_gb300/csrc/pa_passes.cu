@@ -763,7 +763,6 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     constexpr int RL = P::RA, NSL = L / RL;
     constexpr int KR = KEEP8 * RL / 8;
     static_assert(KEEP8 >= 1 && KEEP8 <= 8 && KR * 8 == KEEP8 * RL, "KEEP8 must split the last radix evenly");
-    constexpr int QB = P::NSTAGE == 2 ? E / P::RB : 0;
     constexpr int QL = E / RL;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ float2 tws[QL][NT];  // last-stage per-thread twiddle bases (the second stage reads tab2)
