@@ -148,10 +148,12 @@ int exact_block(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const 
 }
 
 int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const BlockGeom& g, uint32_t flags,
-                 uint32_t* d_out, cudaStream_t s) {
+                 uint32_t* d_out, cudaStream_t s, cudaEvent_t kr_ready = nullptr) {
     if (!e->seed_valid || e->seed_left == 0) return PA_ERR_NO_SEED;
     if (g.n != e->seed_n) return PA_ERR_INVALID_ARG;
     e->last_chunked = false;
+    if (kr_ready && ((flags & PA_FLAG_EXACT) || g.exact_only))  // these paths read key_rest early
+        PA_CUDA(e, cudaStreamWaitEvent(s, kr_ready, 0));
     if (flags & PA_FLAG_EXACT) {
         PA_CUDA(e, cudaEventRecord(e->ev0, s));
         int rc = exact_block(e, d_ks, d_kr, g, flags, d_out, s);
@@ -187,7 +189,7 @@ int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const
         e->tev_count = std::min(e->tev_count + 1, e->tev.size());
     }
     int rc = pa::launch_key_block(g, d_ks, d_kr, flags, e->d_spec, scratch(e), e->d_cnt, e->d_resid, d_out,
-                                  e->num_sms, s, sev);
+                                  e->num_sms, s, sev, kr_ready);
     if (rc) return cuda_fail(e, (cudaError_t)rc);
     PA_CUDA(e, cudaEventRecord(e->ev1, s));
     if (e->seed_left > 0) --e->seed_left;
@@ -282,6 +284,9 @@ int pa_create(const pa_config* cfg, pa_engine** out) {
     if ((err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(err);
     if ((err = cudaEventCreate(&e->ev0)) != cudaSuccess) return fail(err);
     if ((err = cudaEventCreate(&e->ev1)) != cudaSuccess) return fail(err);
+    if ((err = cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking)) != cudaSuccess) return fail(err);
+    if ((err = cudaEventCreateWithFlags(&e->kr_ready, cudaEventDisableTiming)) != cudaSuccess) return fail(err);
+    if ((err = cudaEventCreateWithFlags(&e->main_ready, cudaEventDisableTiming)) != cudaSuccess) return fail(err);
     size_t np = 1ull << e->cap_log_np;
     size_t words = np / 32 + 64;
     if ((err = cudaMalloc(&e->d_key_start, words * 4)) != cudaSuccess) return fail(err);
@@ -326,6 +331,9 @@ void pa_destroy(pa_engine* e) {
         for (auto ev : a) cudaEventDestroy(ev);
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->kr_ready) cudaEventDestroy(e->kr_ready);
+    if (e->main_ready) cudaEventDestroy(e->main_ready);
+    if (e->side) cudaStreamDestroy(e->side);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
@@ -379,10 +387,21 @@ int pa_process(pa_engine* e, const uint32_t* key_start, const uint32_t* key_rest
     PA_CUDA(e, cudaSetDevice(e->device));
     cudaStream_t s = e->stream;
     PA_CUDA(e, cudaMemcpyAsync(e->d_key_start, key_start, (size_t)(g.h / 32u + 1u) * 4u, cudaMemcpyHostToDevice, s));
-    if (flags & PA_FLAG_XOR_KEY_REST)
-        PA_CUDA(e, cudaMemcpyAsync(e->d_key_rest, key_rest, (size_t)(v / 32u) * 4u, cudaMemcpyHostToDevice, s));
-    rc = block_common(e, e->d_key_start, e->d_key_rest, g, flags, e->d_out, s);
-    if (rc) return rc;
+    // key_rest is first read by the block's last kernel: it is copied on the side stream (after
+    // whatever the engine stream had queued) while the passes run
+    cudaEvent_t kr_ready = nullptr;
+    if (flags & PA_FLAG_XOR_KEY_REST) {
+        PA_CUDA(e, cudaEventRecord(e->main_ready, s));
+        PA_CUDA(e, cudaStreamWaitEvent(e->side, e->main_ready, 0));
+        PA_CUDA(e, cudaMemcpyAsync(e->d_key_rest, key_rest, (size_t)(v / 32u) * 4u, cudaMemcpyHostToDevice, e->side));
+        PA_CUDA(e, cudaEventRecord(e->kr_ready, e->side));
+        kr_ready = e->kr_ready;
+    }
+    rc = block_common(e, e->d_key_start, e->d_key_rest, g, flags, e->d_out, s, kr_ready);
+    if (rc) {
+        if (kr_ready) cudaStreamSynchronize(e->side);  // the caller's key_rest is not read after we return
+        return rc;
+    }
     size_t ob = pa_output_bytes(n, v, flags);
     PA_CUDA(e, cudaStreamSynchronize(s));
     float resid = 0.f;

@@ -18,6 +18,9 @@ struct pa_engine {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    // pa_process copies key_rest on `side` while the block's passes run; the finish waits on kr_ready
+    cudaStream_t side = nullptr;
+    cudaEvent_t kr_ready = nullptr, main_ready = nullptr;
     uint32_t max_n = 0;
     int cap_log_np = 0;  // largest cyclic length the buffers hold
     float residual_limit = 0.25f;

@@ -267,12 +267,13 @@ int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec,
 
 int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32_t* key_rest, uint32_t flags,
                      const float2* spec, const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits,
-                     uint32_t* out_words, int num_sms, cudaStream_t s, cudaEvent_t* ev) {
+                     uint32_t* out_words, int num_sms, cudaStream_t s, cudaEvent_t* ev, cudaEvent_t key_rest_ready) {
     auto mark = [&](int i) {
         if (ev) cudaEventRecord(ev[i], s);
     };
     cudaMemsetAsync(resid_bits, 0, sizeof(unsigned int), s);
     if (g.log_n1 == 0) {
+        if (key_rest_ready) cudaStreamWaitEvent(s, key_rest_ready, 0);
         mark(0);
         int rc;
 #define C(NN) mono_key<NN>(g, key_start, key_rest, flags, spec, cnt, resid_bits, out_words, s)
@@ -290,6 +291,7 @@ int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32
     mark(2);
     if (!rc) rc = launch_pass_c(g, *sc.maps, sc.work2, cnt, sc.planes, resid_bits, sc.err, num_sms, s);
     mark(3);
+    if (!rc && key_rest_ready) rc = (int)cudaStreamWaitEvent(s, key_rest_ready, 0);  // key_rest copied meanwhile
     if (!rc) rc = launch_finish(g, sc.planes, key_rest, flags, out_words, s);
     mark(4);
     return rc;

@@ -53,10 +53,12 @@ int launch_seed_spectrum(const BlockGeom& g, const uint32_t* seed, float2* spec,
                          unsigned long long* cnt_seed, int num_sms, cudaStream_t s);
 // Key block: out_words receives ceil(out_bits/32) little-endian words of the reference byte stream.
 // stage_ev (optional, kernel_count_key_block()+1 events) is recorded before the first kernel and
-// after each stage.
+// after each stage.  key_rest_ready (optional): the stream waits on it before the first kernel that
+// reads key_rest (k_finish, or the single-CTA kernel), so key_rest may still be arriving meanwhile.
 int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32_t* key_rest, uint32_t flags,
                      const float2* spec, const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits,
-                     uint32_t* out_words, int num_sms, cudaStream_t s, cudaEvent_t* stage_ev);
+                     uint32_t* out_words, int num_sms, cudaStream_t s, cudaEvent_t* stage_ev,
+                     cudaEvent_t key_rest_ready = nullptr);
 int kernel_count_key_block(const BlockGeom& g);   // kernels one key block launches
 int stage_count_key_block(const BlockGeom& g);    // timed stages (events - 1) of a key block
 
