@@ -89,6 +89,18 @@ def test_pass_c_output_share_variants(gpu_engine, v, flags, split):
     assert np.array_equal(out, O.ntt(seed, ks, kr, n, v, flags))
 
 
+# n = 2^24 (rows 2^14, columns 2^9): key bit rows and the final transpose run in their tiled forms
+# (256 x 256 blocks through shared memory).  Output ratios and flags change which plane words and
+# key_rest words the finish reads.
+@pytest.mark.parametrize("v,flags", [
+    ((1 << 22) + (1 << 21), DEFAULT), ((1 << 22) + 32, pa.FLAG_COMPRESS), ((1 << 23) - 4096, 0),
+    ((1 << 21) + 96, pa.FLAG_XOR_KEY_REST)])
+def test_tiled_transposes_vs_ntt(gpu_engine, v, flags):
+    n = 1 << 24
+    seed, ks, kr, out = run_block(gpu_engine, n, v, 0x71E + v + flags, flags)
+    assert np.array_equal(out, O.ntt(seed, ks, kr, n, v, flags))
+
+
 @pytest.mark.parametrize("n,v,flags", [
     (1 << 16, 24576, 0), (1 << 16, 24576, pa.FLAG_COMPRESS), (1 << 16, 24576, pa.FLAG_XOR_KEY_REST),
     (1 << 16, 61440, DEFAULT), (1 << 16, 32, DEFAULT), (1 << 16, 65504, DEFAULT), (1 << 16, 32768, 0),
