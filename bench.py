@@ -441,7 +441,7 @@ def run_ours(args):
     # ---------------------------------------------------------------- roofline of the dominant kernel
     names = ["pass_a", "pass_b", "pass_c", "finish"]
     n = N_BITS
-    # algorithmic bytes per launch ("Kernels"): the minimum HBM traffic of each pass
+    # algorithmic bytes per launch: the minimum HBM traffic of each pass
     algo = {
         "pass_a": 4 * n + (H_BITS + 1) // 8,        # key bits in, Y (n/2 complex64) out
         "pass_b": 12 * n,                           # Y in, seed spectrum in, Y out

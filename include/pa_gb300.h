@@ -202,9 +202,10 @@ PA_API int pa_autotune(pa_engine* e, uint32_t min_n, uint32_t max_n, float* ms_o
  * multiple of 4.  Work is queued on `stream` (a cudaStream_t; NULL = the legacy default stream) and the
  * call returns without synchronising; no statistics are produced and the precision guard does not run.
  * Limit: n <= 32768 (padded cyclic length <= 32768); larger n returns PA_ERR_TOO_LARGE, and
- * PA_FLAG_EXACT returns PA_ERR_INVALID_ARG.  The scratch (132 KiB) is a static device array of the
- * library, one per GPU: the first call on a device looks up its address (make it before any stream
- * capture), and calls that overlap on one GPU race on it. */
+ * PA_FLAG_EXACT returns PA_ERR_INVALID_ARG.  The scratch (128 KiB + 256 B = 131,328 bytes) is a static
+ * device array of the library, one per GPU: every call looks up its address in the current context (the
+ * first call in a context also loads the library's device code, so make it before any stream capture),
+ * and calls that overlap on one GPU race on it. */
 PA_API int pa_process_noalloc(const uint32_t* d_seed_words, const uint32_t* d_key_start, const uint32_t* d_key_rest,
                               uint32_t n, uint32_t v, uint32_t flags, uint8_t* d_out, void* stream);
 

@@ -7,6 +7,7 @@ Three restatements of the same arithmetic (paths relative to the nicoboss/Privac
 
 * ``direct``   -- C, bit-packed rows (AND + parity), ``oracle/pa_oracle.c``
 * ``ntt``      -- C, exact integer cyclic convolution modulo 2^64-2^32+1, ``oracle/pa_oracle.c``
+  (``NttSeed`` keeps a seed's transform for many keys)
 * ``numpy_reference`` -- pure numpy, small n only; follows the same reference lines:
   bit order ``PrivacyAmplification.cu:223-257,584-593``; key split ``PrivacyAmplification.cu:861-892``;
   convolution ``PrivacyAmplification.cu:1898-1979``; rounding/XOR/packing
@@ -63,6 +64,13 @@ def _load():
                                                  ctypes.c_uint64, ctypes.POINTER(ctypes.c_int64),
                                                  ctypes.c_int]
             lib.pa_oracle_conv_exact.restype = ctypes.c_int
+            lib.pa_oracle_ntt_seed_prepare.argtypes = [u32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
+            lib.pa_oracle_ntt_seed_prepare.restype = ctypes.c_void_p
+            lib.pa_oracle_ntt_seed_free.argtypes = [ctypes.c_void_p]
+            lib.pa_oracle_ntt_seed_free.restype = None
+            lib.pa_oracle_ntt_with_seed.argtypes = [ctypes.c_void_p, u32p, u32p, ctypes.c_uint32, u8p,
+                                                    ctypes.c_int]
+            lib.pa_oracle_ntt_with_seed.restype = ctypes.c_int
             lib.pa_oracle_popcount.argtypes = [u32p, ctypes.c_uint64]
             lib.pa_oracle_popcount.restype = ctypes.c_uint64
             lib.pa_oracle_direct_prepare.argtypes = [u32p, u32p, ctypes.c_uint32, ctypes.c_uint32]
@@ -127,6 +135,34 @@ def ntt(seed, key_start, key_rest, n, v, flags=FLAG_XOR_KEY_REST | FLAG_COMPRESS
     if rc:
         raise ValueError("oracle rejected sizes n=%d v=%d" % (n, v))
     return out
+
+
+class NttSeed:
+    """A seed's exact transform for blocks of size (n, v), kept for many keys (the static-seed case:
+    each block then costs one forward and one inverse transform)."""
+
+    def __init__(self, seed, n, v, threads=0):
+        self._seed = np.ascontiguousarray(seed, dtype=np.uint32)
+        self.n, self.v = n, v
+        self._ctx = _load().pa_oracle_ntt_seed_prepare(_p32(self._seed), n, v, threads)
+        if not self._ctx:
+            raise ValueError("oracle rejected sizes n=%d v=%d" % (n, v))
+
+    def block(self, key_start, key_rest, flags=FLAG_XOR_KEY_REST | FLAG_COMPRESS, threads=0) -> np.ndarray:
+        key_start = np.ascontiguousarray(key_start, dtype=np.uint32)
+        kr = np.ascontiguousarray(key_rest if key_rest is not None else np.zeros(1, np.uint32), dtype=np.uint32)
+        out = np.zeros(out_bits(self.n, self.v, flags) // 8, dtype=np.uint8)
+        if _load().pa_oracle_ntt_with_seed(self._ctx, _p32(key_start), _p32(kr), flags, _p8(out), threads):
+            raise ValueError("oracle failed")
+        return out
+
+    def close(self):
+        if self._ctx:
+            _load().pa_oracle_ntt_seed_free(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        self.close()
 
 
 def conv_exact(seed, key_start, n, v, count, threads=0) -> np.ndarray:

@@ -194,21 +194,27 @@ int pa_oracle_direct(const uint32_t *seed, const uint32_t *key_start, const uint
 
 /* ---------------------------------------------------------------- (b) exact NTT ---------------- */
 
-#define GP 0xFFFFFFFF00000001ull /* 2^64 - 2^32 + 1 */
+/* Arithmetic modulo p = 2^64 - 2^32 + 1, values kept canonical in [0, p).  2^64 = 2^32 - 1 and
+ * 2^96 = -1 (mod p), so a 128-bit product reduces with shifts, one multiply by 2^32 - 1 and carries
+ * (no division). */
+#define GP 0xFFFFFFFF00000001ull
+#define GEPS 0xFFFFFFFFull /* 2^64 mod p */
 
 static inline uint64_t gadd(uint64_t a, uint64_t b) {
     uint64_t s = a + b;
-    if (s < a || s >= GP) s -= GP;
-    return s;
+    if (s < a) return s + GEPS; /* wrapped past 2^64: add 2^64 mod p back; stays below p */
+    return s >= GP ? s - GP : s;
 }
-static inline uint64_t gsub(uint64_t a, uint64_t b) { return a >= b ? a - b : a + (GP - b); }
+static inline uint64_t gsub(uint64_t a, uint64_t b) { return a >= b ? a - b : a - b + GP; }
 static inline uint64_t gred(unsigned __int128 x) {
-    /* 2^64 = 2^32 - 1 and 2^96 = -1 (mod p) */
     uint64_t lo = (uint64_t)x, hi = (uint64_t)(x >> 64);
-    uint64_t hh = hi >> 32, hl = hi & 0xFFFFFFFFull;
-    uint64_t t = gsub(lo % GP, hh % GP);
-    uint64_t u = hl * 0xFFFFFFFFull; /* < 2^64, may exceed p */
-    return gadd(t, u % GP);
+    uint64_t hh = hi >> 32, hl = hi & GEPS;
+    uint64_t t = lo - hh;          /* lo + hl 2^64 + hh 2^96 = lo - hh + hl (2^32 - 1) */
+    if (lo < hh) t -= GEPS;        /* borrow: the wrapped value holds an extra 2^64 = 2^32 - 1 */
+    uint64_t u = hl * GEPS;        /* < 2^64 */
+    uint64_t r = t + u;
+    if (r < u) r += GEPS;          /* carry: 2^64 = 2^32 - 1 again; cannot wrap twice */
+    return r >= GP ? r - GP : r;
 }
 static inline uint64_t gmul(uint64_t a, uint64_t b) { return gred((unsigned __int128)a * b); }
 static uint64_t gpow(uint64_t a, uint64_t e) {
@@ -220,42 +226,213 @@ static uint64_t gpow(uint64_t a, uint64_t e) {
     }
     return r;
 }
+/* Primitive len-th root of unity (len a power of two <= 2^32); 7 generates the multiplicative group. */
+static uint64_t groot(uint64_t len, int inverse) {
+    uint64_t w = gpow(7, (GP - 1) / len);
+    return inverse ? gpow(w, GP - 2) : w;
+}
 
-/* In-place iterative radix-2 NTT of length L (power of two <= 2^32), natural order in and out. */
-static void ntt(uint64_t *a, uint64_t L, int inverse) {
-    for (uint64_t i = 1, j = 0; i < L; ++i) {
-        uint64_t bit = L >> 1;
-        for (; j & bit; bit >>= 1) j ^= bit;
-        j ^= bit;
-        if (i < j) { uint64_t t = a[i]; a[i] = a[j]; a[j] = t; }
+/* Transforms are cache-blocked: layers whose butterfly span fits a block of NTT_BLOCK values run block
+ * by block (one pass over memory for all of them), the wider layers one pass each.  Twiddles of the
+ * narrow layers come from per-length tables (tab[len/2 + k] = w_len^k), those of the wide layers are
+ * formed by repeated multiplication, which is exact in the field. */
+#define NTT_LOG_BLOCK 14
+#define NTT_BLOCK (1ull << NTT_LOG_BLOCK)
+
+typedef struct {
+    uint64_t fwd[NTT_BLOCK], inv[NTT_BLOCK];
+} root_tables;
+
+static root_tables *g_roots;
+
+static const root_tables *roots(void) {
+    root_tables *r = __atomic_load_n(&g_roots, __ATOMIC_ACQUIRE);
+    if (r) return r;
+    r = (root_tables *)malloc(sizeof(root_tables));
+    r->fwd[0] = r->inv[0] = 0;
+    for (uint64_t len = 2; len <= NTT_BLOCK; len <<= 1) {
+        uint64_t w = groot(len, 0), wi = groot(len, 1), a = 1, b = 1;
+        for (uint64_t k = 0; k < len / 2; ++k) {
+            r->fwd[len / 2 + k] = a;
+            r->inv[len / 2 + k] = b;
+            a = gmul(a, w);
+            b = gmul(b, wi);
+        }
     }
-    for (uint64_t len = 2; len <= L; len <<= 1) {
-        /* 7 generates the multiplicative group of GP */
-        uint64_t w = gpow(7, (GP - 1) / len);
-        if (inverse) w = gpow(w, GP - 2);
-        uint64_t half = len >> 1;
-        uint64_t *tw = (uint64_t *)malloc(half * 8);
-        tw[0] = 1;
-        for (uint64_t k = 1; k < half; ++k) tw[k] = gmul(tw[k - 1], w);
+    root_tables *expected = NULL;
+    if (!__atomic_compare_exchange_n(&g_roots, &expected, r, 0, __ATOMIC_ACQ_REL, __ATOMIC_ACQUIRE)) {
+        free(r);
+        return expected;
+    }
+    return r;
+}
+
+/* One wide layer (butterfly span half = len/2 over the whole array), parallel over butterflies. */
+static void wide_layer(uint64_t *a, uint64_t L, uint64_t len, int inverse) {
+    const uint64_t half = len >> 1, w = groot(len, inverse), total = L >> 1;
 #ifdef _OPENMP
-#pragma omp parallel for schedule(static) if (L >= (1u << 16))
+#pragma omp parallel
 #endif
-        for (int64_t s = 0; s < (int64_t)L; s += (int64_t)len) {
-            for (uint64_t k = 0; k < half; ++k) {
-                uint64_t x = a[s + k], y = gmul(a[s + k + half], tw[k]);
-                a[s + k] = gadd(x, y);
-                a[s + k + half] = gsub(x, y);
+    {
+        uint64_t nt = 1, id = 0;
+#ifdef _OPENMP
+        nt = (uint64_t)omp_get_num_threads();
+        id = (uint64_t)omp_get_thread_num();
+#endif
+        uint64_t j0 = total * id / nt, j1 = total * (id + 1) / nt;
+        uint64_t k = j0 % half, s = (j0 / half) * len;
+        uint64_t wk = gpow(w, k);
+        for (uint64_t j = j0; j < j1; ++j) {
+            uint64_t *x = a + s + k, *y = x + half;
+            if (!inverse) { /* DIF: (u + v, (u - v) w^k) */
+                uint64_t u = *x, v = *y;
+                *x = gadd(u, v);
+                *y = gmul(gsub(u, v), wk);
+            } else { /* DIT: (u + v w^-k, u - v w^-k) */
+                uint64_t u = *x, v = gmul(*y, wk);
+                *x = gadd(u, v);
+                *y = gsub(u, v);
+            }
+            wk = gmul(wk, w);
+            if (++k == half) {
+                k = 0;
+                s += len;
+                wk = 1;
             }
         }
-        free(tw);
     }
-    if (inverse) {
-        uint64_t inv = gpow(L % GP, GP - 2);
+}
+
+/* All layers with len <= min(L, NTT_BLOCK) on each block of that size. */
+static void narrow_layers(uint64_t *a, uint64_t L, int inverse) {
+    const root_tables *rt = roots();
+    const uint64_t B = L < NTT_BLOCK ? L : NTT_BLOCK;
+    const uint64_t *tab = inverse ? rt->inv : rt->fwd;
 #ifdef _OPENMP
-#pragma omp parallel for schedule(static) if (L >= (1u << 16))
+#pragma omp parallel for schedule(static) if (L > B)
 #endif
-        for (int64_t i = 0; i < (int64_t)L; ++i) a[i] = gmul(a[i], inv);
+    for (int64_t b = 0; b < (int64_t)(L / B); ++b) {
+        uint64_t *x = a + (uint64_t)b * B;
+        if (!inverse) {
+            for (uint64_t len = B; len >= 2; len >>= 1) {
+                const uint64_t half = len >> 1, *w = tab + half;
+                for (uint64_t s = 0; s < B; s += len)
+                    for (uint64_t k = 0; k < half; ++k) {
+                        uint64_t u = x[s + k], v = x[s + k + half];
+                        x[s + k] = gadd(u, v);
+                        x[s + k + half] = gmul(gsub(u, v), w[k]);
+                    }
+            }
+        } else {
+            for (uint64_t len = 2; len <= B; len <<= 1) {
+                const uint64_t half = len >> 1, *w = tab + half;
+                for (uint64_t s = 0; s < B; s += len)
+                    for (uint64_t k = 0; k < half; ++k) {
+                        uint64_t u = x[s + k], v = gmul(x[s + k + half], w[k]);
+                        x[s + k] = gadd(u, v);
+                        x[s + k + half] = gsub(u, v);
+                    }
+            }
+        }
     }
+}
+
+/* Forward transform, natural order in, bit-reversed order out (decimation in frequency). */
+static void ntt_dif(uint64_t *a, uint64_t L) {
+    for (uint64_t len = L; len > NTT_BLOCK; len >>= 1) wide_layer(a, L, len, 0);
+    narrow_layers(a, L, 0);
+}
+
+/* Inverse transform without the 1/L factor, bit-reversed order in, natural order out (decimation in
+ * time): ntt_dit(ntt_dif(x)) = L x. */
+static void ntt_dit(uint64_t *a, uint64_t L) {
+    narrow_layers(a, L, 1);
+    for (uint64_t len = 2 * NTT_BLOCK; len <= L; len <<= 1) wide_layer(a, L, len, 1);
+}
+
+/* Transform length: n for power-of-two n (cyclic), else the next power of two >= n + h + 1 (a linear
+ * convolution, folded mod n afterwards). */
+static uint64_t conv_length(uint32_t n, uint32_t h) {
+    int pow2 = (n & (n - 1u)) == 0;
+    uint64_t L = 1, need = pow2 ? n : (uint64_t)n + h + 1u;
+    while (L < need) L <<= 1;
+    return L;
+}
+
+/* A seed's transform for blocks of size (n, v), scaled by 1/L so that one product and the inverse
+ * transform give the convolution. */
+typedef struct {
+    uint32_t n, v, h;
+    uint64_t L;
+    uint64_t *S;
+} ntt_seed;
+
+static void set_threads(int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+}
+
+void *pa_oracle_ntt_seed_prepare(const uint32_t *seed, uint32_t n, uint32_t v, int nthreads) {
+    if (n == 0 || (n & 31u) || v >= n) return NULL;
+    set_threads(nthreads);
+    ntt_seed *c = (ntt_seed *)calloc(1, sizeof(ntt_seed));
+    c->n = n;
+    c->v = v;
+    c->h = n - v;
+    c->L = conv_length(n, c->h);
+    c->S = (uint64_t *)malloc(c->L * 8);
+    if (!c->S) { free(c); return NULL; }
+    const uint64_t L = c->L;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t m = 0; m < (int64_t)L; ++m) c->S[m] = (uint64_t)m < n ? bit_msb(seed, (uint64_t)m) : 0u;
+    ntt_dif(c->S, L);
+    const uint64_t linv = gpow(L % GP, GP - 2);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t i = 0; i < (int64_t)L; ++i) c->S[i] = gmul(c->S[i], linv);
+    return c;
+}
+
+void pa_oracle_ntt_seed_free(void *ctx) {
+    ntt_seed *c = (ntt_seed *)ctx;
+    if (!c) return;
+    free(c->S);
+    free(c);
+}
+
+/* c[i] = sum_{j=0..h} key_start[j] * seed[(i-j) mod n] for i < count, exact, into conv (count values). */
+static int conv_with_seed(const ntt_seed *c, const uint32_t *key_start, uint64_t count, int64_t *conv) {
+    const uint64_t L = c->L, n = c->n, h = c->h;
+    const int pow2 = (c->n & (c->n - 1u)) == 0;
+    if (count > n) return -1;
+    uint64_t *A = (uint64_t *)malloc(L * 8);
+    if (!A) return -1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t j = 0; j < (int64_t)L; ++j) A[j] = (uint64_t)j <= h ? bit_msb(key_start, (uint64_t)j) : 0u;
+    ntt_dif(A, L);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t i = 0; i < (int64_t)L; ++i) A[i] = gmul(A[i], c->S[i]);
+    ntt_dit(A, L);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t i = 0; i < (int64_t)count; ++i) {
+        uint64_t v = A[i];
+        if (!pow2 && (uint64_t)i + n < L) v += A[(uint64_t)i + n];
+        conv[i] = (int64_t)v;
+    }
+    free(A);
+    return 0;
 }
 
 /* Exact cyclic convolution c[i] = sum_{j=0..h} key_start[j] * seed[(i-j) mod n] for i < count.
@@ -264,31 +441,45 @@ static void ntt(uint64_t *a, uint64_t L, int inverse) {
 int pa_oracle_conv_exact(const uint32_t *seed, const uint32_t *key_start, uint32_t n, uint32_t v,
                          uint64_t count, int64_t *conv, int nthreads) {
     if (n == 0 || (n & 31u) || v >= n || count > n) return -1;
+    ntt_seed *c = (ntt_seed *)pa_oracle_ntt_seed_prepare(seed, n, v, nthreads);
+    if (!c) return -1;
+    int rc = conv_with_seed(c, key_start, count, conv);
+    pa_oracle_ntt_seed_free(c);
+    return rc;
+}
+
+/* Output bytes from the exact convolution values: bit i = c[i] mod 2 (XOR key_rest bit i for i < v when
+ * PA_FLAG_XOR_KEY_REST), byte i/8, bit 7 - i%8.  ob is a multiple of 8. */
+static void emit_parity(const int64_t *c, uint64_t ob, const uint32_t *key_rest, uint32_t v, uint32_t flags,
+                        uint8_t *out) {
+    const int x = (flags & PA_FLAG_XOR_KEY_REST) && key_rest;
 #ifdef _OPENMP
-    if (nthreads > 0) omp_set_num_threads(nthreads);
-#else
-    (void)nthreads;
+#pragma omp parallel for schedule(static)
 #endif
-    uint32_t h = n - v;
-    int pow2 = (n & (n - 1u)) == 0;
-    uint64_t L = 1;
-    uint64_t need = pow2 ? n : (uint64_t)n + h + 1u;
-    while (L < need) L <<= 1;
-    uint64_t *A = (uint64_t *)calloc(L, 8), *B = (uint64_t *)calloc(L, 8);
-    if (!A || !B) { free(A); free(B); return -1; }
-    for (uint64_t j = 0; j <= h; ++j) A[j] = bit_msb(key_start, j);
-    for (uint64_t m = 0; m < n; ++m) B[m] = bit_msb(seed, m);
-    ntt(A, L, 0);
-    ntt(B, L, 0);
-    for (uint64_t i = 0; i < L; ++i) A[i] = gmul(A[i], B[i]);
-    ntt(A, L, 1);
-    for (uint64_t i = 0; i < count; ++i) {
-        uint64_t c = A[i];
-        if (!pow2 && i + n < L) c += A[i + n];
-        conv[i] = (int64_t)c;
+    for (int64_t b = 0; b < (int64_t)(ob / 8); ++b) {
+        uint32_t byte = 0;
+        for (uint32_t t = 0; t < 8; ++t) {
+            uint64_t i = 8u * (uint64_t)b + t;
+            uint32_t bit = (uint32_t)(c[i] & 1);
+            if (x && i < v) bit ^= bit_msb(key_rest, i);
+            byte |= bit << (7u - t);
+        }
+        out[b] = (uint8_t)byte;
     }
-    free(A);
-    free(B);
+}
+
+/* Full block with a prepared seed transform (pa_oracle_ntt_seed_prepare for the same n, v). */
+int pa_oracle_ntt_with_seed(void *ctx, const uint32_t *key_start, const uint32_t *key_rest, uint32_t flags,
+                            uint8_t *out, int nthreads) {
+    ntt_seed *c = (ntt_seed *)ctx;
+    if (!c) return -1;
+    set_threads(nthreads);
+    uint64_t ob = pa_oracle_out_bits(c->n, c->v, flags);
+    int64_t *conv = (int64_t *)malloc(ob * 8);
+    if (!conv) return -1;
+    if (conv_with_seed(c, key_start, ob, conv)) { free(conv); return -1; }
+    emit_parity(conv, ob, key_rest, c->v, flags, out);
+    free(conv);
     return 0;
 }
 
@@ -296,16 +487,11 @@ int pa_oracle_conv_exact(const uint32_t *seed, const uint32_t *key_start, uint32
 int pa_oracle_ntt(const uint32_t *seed, const uint32_t *key_start, const uint32_t *key_rest, uint32_t n,
                   uint32_t v, uint32_t flags, uint8_t *out, int nthreads) {
     if (n == 0 || (n & 31u) || (v & 31u) || v == 0 || v >= n) return -1;
-    uint64_t ob = pa_oracle_out_bits(n, v, flags);
-    int64_t *c = (int64_t *)malloc(ob * 8);
+    void *c = pa_oracle_ntt_seed_prepare(seed, n, v, nthreads);
     if (!c) return -1;
-    if (pa_oracle_conv_exact(seed, key_start, n, v, ob, c, nthreads)) { free(c); return -1; }
-    uint8_t *par = (uint8_t *)malloc(ob);
-    for (uint64_t i = 0; i < ob; ++i) par[i] = (uint8_t)(c[i] & 1);
-    free(c);
-    emit_bits(par, 0, ob, key_rest, v, flags, out);
-    free(par);
-    return 0;
+    int rc = pa_oracle_ntt_with_seed(c, key_start, key_rest, flags, out, nthreads);
+    pa_oracle_ntt_seed_free(c);
+    return rc;
 }
 
 /* Popcount of the first `bits` bits of an MSB-first word array (the Hamming weights that

@@ -16,7 +16,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
 
 namespace {
 
@@ -27,22 +26,15 @@ constexpr size_t kScratchBytes = kSpecBytes + 256;                       // + po
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Device address of g_noalloc_scratch per device.  In host code the symbol is only a host-side stand-in,
-// so the address comes from cudaGetSymbolAddress, once per device with that device current.
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
-
+// Device address of g_noalloc_scratch in the current context.  In host code the symbol is only a
+// host-side stand-in, so the address comes from cudaGetSymbolAddress with the caller's device current.
+// It is looked up on every call rather than cached: after a cudaDeviceReset, or under a context the
+// caller made current itself, the library's device code is loaded again and the array moves.  The
+// lookup costs about a microsecond; the first one in a context also loads the library's device code.
 int scratch_address(void** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PA_ERR_CUDA;
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return PA_ERR_CUDA;
-        g_addr[dev] = p;
-    }
-    *out = g_addr[dev];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return PA_ERR_CUDA;
+    *out = p;
     return PA_OK;
 }
 

@@ -11,7 +11,8 @@ nicoboss/PrivacyAmplification.  It holds
 * ``amp_out_pre_hash``, ``key_rest_hash``, ``amp_out_reult`` (Matrix.h:533,540,547) -- the n=2^14
   (v=6144, h=10240) composite before the key_rest XOR, the key_rest bytes, and the final result.
 
-Usage: python tests/golden/make_golden.py [path/to/Matrix.h]
+Usage: python tests/golden/make_golden.py path/to/Matrix.h
+       (or PA_REFERENCE_TREE=<root of the reference tree> python tests/golden/make_golden.py)
 The fixture is committed; this script only has to be re-run if the source changes.
 """
 import os
@@ -20,7 +21,7 @@ import sys
 
 import numpy as np
 
-DEFAULT_SRC = "/root/reference/examples/LargeBlocksizeExample/Matrix.h"
+MATRIX_H = os.path.join("examples", "LargeBlocksizeExample", "Matrix.h")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "large_block_kat.npz")
 
 
@@ -54,4 +55,9 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_SRC)
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    elif os.environ.get("PA_REFERENCE_TREE"):
+        main(os.path.join(os.environ["PA_REFERENCE_TREE"], MATRIX_H))
+    else:
+        raise SystemExit(__doc__)

@@ -53,7 +53,7 @@ def small_engine(pa_lib):
 
 @pytest.mark.parametrize("n,v,flags", [
     (1 << 15, 12288, DEFAULT), (1 << 14, 6144, 0), (1 << 10, 384, DEFAULT), (1 << 15, 4096, pa.FLAG_COMPRESS),
-    (20480, 7680, DEFAULT), (1056, 480, 0)])
+    (20480, 7680, DEFAULT), (1056, 480, 0), (1 << 10, 32, DEFAULT), (1 << 10, 992, pa.FLAG_COMPRESS)])
 def test_two_calls_in_a_row_match_pa_process(torch_cuda, small_engine, n, v, flags):
     """Two different blocks queued back to back on one stream: each equals pa_process on the same inputs
     (so nothing of the first call leaks into the second through the shared scratch)."""
