@@ -143,42 +143,55 @@ def make_inputs(nkeys):
     return seed, keys
 
 
-def cpu_sample(seconds, cores, seed_no=0x5EED):
-    """Direct bit-packed oracle on a row sample of the bench block.  Returns (block seconds
-    extrapolated to all v rows, sample description): per-block setup (seed reversal, key packing)
-    once, plus v times the measured per-row cost."""
-    from oracle import oracle as O
-    seed, recv = O.random_block(N_BITS, V_BITS, seed_no)
-    ks, _ = O.key_split(recv, N_BITS, V_BITS)
-    t = time.perf_counter()
-    blk = O.DirectBlock(seed, ks, N_BITS, V_BITS)
-    setup = time.perf_counter() - t
-    t = time.perf_counter()
-    blk.rows(0, 512, threads=cores)
-    per_row = (time.perf_counter() - t) / 512
-    rows = int(max(512, min(V_BITS, seconds / max(per_row, 1e-9)))) // 64 * 64
-    t = time.perf_counter()
-    blk.rows(0, rows, threads=cores)
-    t_rows = time.perf_counter() - t
-    blk.close()
-    block_s = setup + V_BITS * (t_rows / rows)
-    sample = ("%d of %d output rows of the n=2^27 block in %.2f s on %d threads, plus the per-block setup "
-              "(%.2f s), extrapolated linearly to all rows" % (rows, V_BITS, t_rows, cores, setup))
-    return block_s, sample
+class CpuBlocks:
+    """The oracle's exact NTT port on the bench workload with the seed transform kept (the static-seed
+    case: the reference caches its seed spectrum the same way), so that one call is one whole key block
+    -- forward transform of the key, product, inverse transform, parity, key_rest XOR, packing -- on
+    `threads` host threads."""
+
+    def __init__(self, threads=0):
+        from oracle import oracle as O
+        self.O = O
+        self.cores = threads or os.cpu_count() or 1
+        seed, _ = O.random_block(N_BITS, V_BITS, 0x5EED)
+        t = time.perf_counter()
+        self.ref = O.NttSeed(seed, N_BITS, V_BITS, threads=self.cores)
+        self.seed_s = time.perf_counter() - t
+        self.keys = []
+        for i in range(KEY_BUFFERS):
+            _, recv = O.random_block(N_BITS, V_BITS, 0x5EED + 1 + i)
+            self.keys.append(O.key_split(recv, N_BITS, V_BITS))
+
+    def block(self, i):
+        """One whole block; returns (seconds, output bytes)."""
+        ks, kr = self.keys[i % len(self.keys)]
+        t = time.perf_counter()
+        out = self.ref.block(ks, kr, threads=self.cores)
+        return time.perf_counter() - t, out
+
+    def close(self):
+        self.ref.close()
 
 
-def cpu_baseline(threads=0):
-    """The fastest CPU restatement in the repo: one whole n=2^27 block by the exact NTT convolution
-    (oracle/pa_oracle.c, OpenMP over butterflies), timed once."""
-    from oracle import oracle as O
-    cores = threads or os.cpu_count() or 1
-    seed, recv = O.random_block(N_BITS, V_BITS, 0x5EED)
-    ks, kr = O.key_split(recv, N_BITS, V_BITS)
-    t = time.perf_counter()
-    O.ntt(seed, ks, kr, N_BITS, V_BITS, threads=cores)
-    dt = time.perf_counter() - t
-    sample = "one whole n=2^27 block (exact NTT convolution mod 2^64-2^32+1) in %.1f s on %d threads" % (dt, cores)
-    return N_BITS / dt / 1e9, cores, sample
+def cpu_baseline(threads=0, blocks=2):
+    """The CPU port timed on whole n=2^27 blocks (the median of `blocks`), seed transform excluded."""
+    cb = CpuBlocks(threads)
+    try:
+        times = [cb.block(i)[0] for i in range(blocks)]
+    finally:
+        cb.close()
+    dt = statistics.median(times)
+    sample = ("%d whole n=2^27 blocks (exact NTT convolution mod 2^64-2^32+1, seed transform kept as in the "
+              "static-seed path; %.1f s once), median %.2f s per block on %d threads"
+              % (blocks, cb.seed_s, dt, cb.cores))
+    return N_BITS / dt / 1e9, cb.cores, sample
+
+
+def workload_config(world):
+    """The `config` of both arms' lines (identical, so that the two lines describe the same workload)."""
+    return {"workload": WORKLOAD, "n": N_BITS, "h": H_BITS, "v": V_BITS, "blocks_per_step": 1,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2: 512 MiB work array + 512 MiB seed spectrum per block"}
 
 
 def cufft_plain_leg(seed, keys, eng, steps):
@@ -250,30 +263,44 @@ def dist_setup():
 
 
 def run_reference(args):
+    """The reference arm: the reference ships no CPU implementation of the path and its CUDA build is not
+    on the GPU host, so this times the CPU port (oracle, exact NTT, all host threads) on the same workload,
+    one whole block per step.  Under torchrun only rank 0 runs it."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
-    cores = os.cpu_count() or 1
-    # each step: one bounded sample (per-block setup + a row sample) of a fresh block, extrapolated
-    per_step = max(0.5, min(3.0, 120.0 / max(1, args.steps + args.warmup)))
-    for i in range(args.warmup):
-        cpu_sample(per_step, cores, 0x5EED + i)
-    results = [cpu_sample(per_step, cores, 0x5EED + 100 + i) for i in range(args.steps)]
-    block_s = statistics.mean(r[0] for r in results)
-    value = N_BITS / block_s / 1e9
-    sample = "per step: " + results[-1][1]
+    cb = CpuBlocks()
+    try:
+        for i in range(args.warmup):
+            cb.block(i)
+        times = [cb.block(args.warmup + i)[0] for i in range(args.steps)]
+    finally:
+        cb.close()
+    total = sum(times)
+    value = args.steps * N_BITS / total / 1e9
+    sample = ("%d whole n=2^27 blocks after %d warm-up blocks, exact NTT convolution mod 2^64-2^32+1 on %d "
+              "threads (seed transform computed once, %.1f s, as the static-seed path caches it); per block "
+              "median %.2f s, min %.2f s, max %.2f s" % (args.steps, args.warmup, cb.cores, cb.seed_s,
+                                                          statistics.median(times), min(times), max(times)))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": block_s * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u1", "data": DATA,
-        "config": {"workload": WORKLOAD, "n": N_BITS, "h": H_BITS, "v": V_BITS,
-                   "implementation": "CPU port of the reference's GF(2) Toeplitz product (oracle/pa_oracle.c, "
-                                     "direct bit-packed rows); the reference itself has no CPU path"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 (mod p)", "data": DATA,
+        "config": workload_config(world),
+        "implementation": "CPU port of the path (oracle/pa_oracle.c: exact NTT convolution, OpenMP); the "
+                          "reference itself has no CPU path",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cb.cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def spread(xs):
+    """Median and spread of repeated measurements."""
+    ys = sorted(xs)
+    return {"median": statistics.median(ys), "min": ys[0], "max": ys[-1], "p10": pct(ys, 10), "p90": pct(ys, 90),
+            "repeats": len(ys)}
 
 
 def run_ours(args):
@@ -292,12 +319,21 @@ def run_ours(args):
     torch.cuda.set_device(local)
     pa_build.build()
     dev = torch.device("cuda", local)
+    R, K = args.repeats, args.steps
+
+    def fence():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
 
     seed, keys = make_inputs(KEY_BUFFERS)
     eng = pa.Engine(max_sample_size=N_BITS, device_id=local)
     eng.set_seed(seed, N_BITS, -1)
 
-    # ---------------------------------------------------------------- device-resident timed region
+    # ---------------------------------------------------------------- device-resident, one stream
+    # The same K blocks one after another through pa_process_device, the timed region repeated R times:
+    # per-block device latency (an event after every block) and the per-kernel times of the roofline.
     d_keys = [(torch.from_numpy(ks.view(np.int32)).to(dev), torch.from_numpy(kr.view(np.int32)).to(dev))
               for ks, kr in keys]
     nbytes_out = pa.output_bytes(N_BITS, V_BITS)
@@ -312,39 +348,34 @@ def run_ours(args):
     for i in range(args.warmup):
         block(i)
     eng.sync()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
+    fence()
     eng.set_timing(True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # one event after every block as well (recording an event adds no work): per-block device times
-    ev_blk = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    with ClockSampler(local) as clk:
-        with torch.cuda.stream(stream):
-            ev0.record(stream)
-            for i in range(args.steps):
-                block(i)
-                ev_blk[i].record(stream)
-            ev1.record(stream)
-        ev1.synchronize()
-        # keep the sampler alive for a short tail so that very short runs still get a sample
-        if args.steps * 1.0 < 200:
-            time.sleep(0.25)
-    torch.cuda.synchronize()
+    ev_blk = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    t_one, blk_ms, stage_sum, stage_n = [], [], None, 0
+    with ClockSampler(local) as clk_one:
+        for rep in range(R):
+            fence()
+            with torch.cuda.stream(stream):
+                ev0.record(stream)
+                for i in range(K):
+                    block(i)
+                    ev_blk[i].record(stream)
+                ev1.record(stream)
+            ev1.synchronize()
+            t_one.append(max_over_ranks([ev0.elapsed_time(ev1) / 1e3], dist, dev)[0])
+            blk_ms += [ev0.elapsed_time(ev_blk[0])] + [ev_blk[i - 1].elapsed_time(ev_blk[i]) for i in range(1, K)]
+            sm, nb = eng.stage_times()
+            stage_sum = [a + b * nb for a, b in zip(stage_sum, sm)] if stage_sum else [b * nb for b in sm]
+            stage_n += nb
     stats = eng.sync()
-    stage_ms, stage_blocks = eng.stage_times()
     eng.set_timing(False)
-    t_dev = max_over_ranks([ev0.elapsed_time(ev1) / 1e3], dist, dev)[0]
-    blk_ms = [ev0.elapsed_time(ev_blk[0])] + [ev_blk[i - 1].elapsed_time(ev_blk[i]) for i in range(1, args.steps)]
-    clk_one = clk
-    if dist:
-        dist.barrier()
+    stage_ms = [x / stage_n for x in stage_sum] if stage_n else []
 
     # ---------------------------------------------------------------- device-resident, blocks in flight
-    # The headline value: the same blocks, IN_FLIGHT at a time (pa_batch_run over that many slots, the
+    # The headline value: the same K blocks, IN_FLIGHT at a time (pa_batch_run over that many slots, the
     # seed spectrum cached once), so that one block's kernel tails and short kernels overlap the next
-    # block's work.  The one-stream run above gives the per-block latency and per-kernel times.
+    # block's work; the timed region repeated R times, value = the median repeat.
     sid = eng.seed_cache_add(seed, N_BITS, V_BITS)
     n_out = 16
     d_outs = [torch.empty((nbytes_out + 3) // 4, dtype=torch.int32, device=dev) for _ in range(n_out)]
@@ -356,18 +387,16 @@ def run_ours(args):
     eng.set_pool(0, 16, IN_FLIGHT)
     eng.batch_run(jobs_for(args.warmup), 0, sh)
     eng.batch_sync(args.warmup)
-    timed_jobs = jobs_for(args.steps)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
+    timed_jobs = jobs_for(K)
+    t_conc = []
     with ClockSampler(local) as clk:
-        eng.batch_run(timed_jobs, 0, sh)
-        bst = eng.batch_sync(args.steps)
-        if args.steps * 1.0 < 200:
-            time.sleep(0.25)
+        for rep in range(R):
+            fence()
+            eng.batch_run(timed_jobs, 0, sh)
+            bst = eng.batch_sync(K)
+            t_conc.append(max_over_ranks([bst[0].gpu_ms / 1e3], dist, dev)[0])
     torch.cuda.synchronize()
-    t_conc = max_over_ranks([bst[0].gpu_ms / 1e3], dist, dev)[0]
-    conc_equal = bool(torch.equal(d_outs[(args.steps - 1) % n_out], d_out))
+    conc_equal = bool(torch.equal(d_outs[(K - 1) % n_out], d_out))
     if dist:
         dist.barrier()
 
@@ -381,20 +410,19 @@ def run_ours(args):
     for i in range(args.warmup):
         ks, kr = pin_keys[i % len(pin_keys)]
         eng.process(ks, kr, N_BITS, V_BITS, out=pin_out)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sync_ms = []
-    for i in range(args.steps):
-        ks, kr = pin_keys[i % len(pin_keys)]
-        t1 = time.perf_counter()
-        eng.process(ks, kr, N_BITS, V_BITS, out=pin_out)
-        sync_ms.append((time.perf_counter() - t1) * 1e3)
-    t_e2e_sync = time.perf_counter() - t0
+    t_e2e_sync, sync_ms = [], []
+    for rep in range(R):
+        fence()
+        t0 = time.perf_counter()
+        for i in range(K):
+            ks, kr = pin_keys[i % len(pin_keys)]
+            t1 = time.perf_counter()
+            eng.process(ks, kr, N_BITS, V_BITS, out=pin_out)
+            sync_ms.append((time.perf_counter() - t1) * 1e3)
+        t_e2e_sync.append(max_over_ranks([time.perf_counter() - t0], dist, dev)[0])
 
-    # pipelined form of the same calls: pa_submit / pa_poll with two blocks in flight, so one block's
-    # host copies overlap the other's kernels (same pinned host buffers, same bytes per block)
+    # pipelined form of the same calls: pa_submit / pa_poll with E2E_IN_FLIGHT blocks in flight, so one
+    # block's host copies overlap the others' kernels (same pinned host buffers, same bytes per block)
     depth = E2E_IN_FLIGHT
     pin_outs = [torch.empty(nbytes_out, dtype=torch.uint8).pin_memory().numpy() for _ in range(depth)]
 
@@ -420,15 +448,14 @@ def run_ours(args):
                 pass
 
     pipelined(args.warmup)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    pipelined(args.steps)
-    t_e2e = time.perf_counter() - t0
-    same_out = bool((pin_outs[(args.steps - 1) % depth] == eng.process(*keys[(args.steps - 1) % len(keys)],
-                                                                       N_BITS, V_BITS)).all())
-    t_e2e, t_e2e_sync = max_over_ranks([t_e2e, t_e2e_sync], dist, dev)
+    t_e2e = []
+    with ClockSampler(local) as clk_e2e:
+        for rep in range(R):
+            fence()
+            t0 = time.perf_counter()
+            pipelined(K)
+            t_e2e.append(max_over_ranks([time.perf_counter() - t0], dist, dev)[0])
+    same_out = bool((pin_outs[(K - 1) % depth] == eng.process(*keys[(K - 1) % len(keys)], N_BITS, V_BITS)).all())
     h2d = (H_BITS // 32 + 1) * 4 + (V_BITS // 32) * 4
     d2h = nbytes_out
 
@@ -458,11 +485,12 @@ def run_ours(args):
         roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": tr, "algorithmic_bytes": algo[top],
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                else "fallback 6.8 TB/s"}
+                else "fallback 6.8 TB/s",
+                "kernel_fracs": {k: algo[k] / (kern[k] / 1e3) / 1e9 / peak for k in kern}}
     block_bytes = 20 * n + ((H_BITS + 1) + 2 * V_BITS) // 8
     total_s = sum(stage_ms) / 1e3 if stage_ms else None
 
-    plain = None if args.no_cufft else cufft_plain_leg(seed, keys, eng, min(args.steps, 20))
+    plain = None if args.no_cufft else cufft_plain_leg(seed, keys, eng, min(K, 20))
 
     if args.no_cpu:
         cpu = None
@@ -470,31 +498,39 @@ def run_ours(args):
         cb, cores, sample = cpu_baseline()
         cpu = {"value": cb, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
 
-    value = job_value(world, args.steps, N_BITS, t_conc)
+    s_conc, s_one, s_e2e, s_sync = spread(t_conc), spread(t_one), spread(t_e2e), spread(t_e2e_sync)
+    gbit = lambda secs: job_value(world, K, N_BITS, secs)
+    value = gbit(s_conc["median"])
+    block_gbs = block_bytes / (s_conc["median"] / K) / 1e9
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_conc / args.steps * 1e3, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": s_conc["median"] / K * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
-        "config": {"workload": WORKLOAD, "n": N_BITS, "h": H_BITS, "v": V_BITS, "blocks_per_step": 1,
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "blocks_in_flight": IN_FLIGHT,
-                   "l2": "inputs larger than L2: 512 MiB work array + 512 MiB seed spectrum per block"},
-        "e2e": {"value": job_value(world, args.steps, N_BITS, t_e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "api": "pa_submit/pa_poll, %d blocks in flight, pinned host buffers" % E2E_IN_FLIGHT,
-                "output_equals_pa_process": same_out,
-                "sync_value": job_value(world, args.steps, N_BITS, t_e2e_sync),
-                "sync_api": "pa_process, one block at a time"},
-        "gpu_launches": args.steps * pa.kernels_per_block(N_BITS, V_BITS),
-        "value_one_stream": {"value": job_value(world, args.steps, N_BITS, t_dev), "unit": UNIT,
+        "config": workload_config(world),
+        "blocks_in_flight": IN_FLIGHT,
+        "repeats": {"count": R, "what": "the K-step timed region is run R times (each bracketed by a sync); "
+                                        "value = median repeat",
+                    "gbit_s": {k: (gbit(v) if k != "repeats" else v) for k, v in s_conc.items()}},
+        "e2e": {"value": gbit(s_e2e["median"]), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "api": "pa_submit/pa_poll, %d blocks in flight, pinned host buffers" % E2E_IN_FLIGHT,
+                "repeats_gbit_s": {k: (gbit(v) if k != "repeats" else v) for k, v in s_e2e.items()},
+                "output_equals_pa_process": same_out, "clocks": clk_e2e.summary(),
+                "sync_value": gbit(s_sync["median"]), "sync_api": "pa_process, one block at a time"},
+        "gpu_launches": K * pa.kernels_per_block(N_BITS, V_BITS),
+        "value_one_stream": {"value": gbit(s_one["median"]), "unit": UNIT,
+                             "repeats_gbit_s": {k: (gbit(v) if k != "repeats" else v) for k, v in s_one.items()},
                              "api": "pa_process_device, one block after another on one stream",
                              "output_equals_in_flight": conc_equal, "clocks": clk_one.summary()},
         "latency_ms": {"device_p50": pct(blk_ms, 50), "device_p99": pct(blk_ms, 99), "device_max": max(blk_ms),
+                       "blocks": len(blk_ms),
                        "pa_process_p50": pct(sync_ms, 50), "pa_process_p99": pct(sync_ms, 99),
                        "what": "device: CUDA events between consecutive blocks on the engine stream; "
                                "pa_process: host wall time of one synchronous call (copies in, block, copy out)"},
-        "kernels_ms": kern, "kernel_blocks_timed": stage_blocks,
-        "block_hbm_model": {"bytes": block_bytes, "GB_per_s_at_kernel_sum": block_bytes / total_s / 1e9
-                            if total_s else None},
+        "kernels_ms": kern, "kernel_blocks_timed": stage_n,
+        "block_hbm_model": {"bytes": block_bytes, "GB_per_s_in_flight": block_gbs,
+                            "frac_in_flight": block_gbs / peak,
+                            "GB_per_s_at_kernel_sum": block_bytes / total_s / 1e9 if total_s else None},
         "roofline": roof,
         "cpu_baseline": cpu,
         "cufft_plain": plain,
@@ -709,8 +745,9 @@ def run_serve(args, static):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--repeats", type=int, default=25, help="runs of the K-step timed region (value: median)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT pipeline baseline leg")

@@ -200,21 +200,22 @@ int pa_oracle_direct(const uint32_t *seed, const uint32_t *key_start, const uint
 #define GP 0xFFFFFFFF00000001ull
 #define GEPS 0xFFFFFFFFull /* 2^64 mod p */
 
+/* Branch-free (masks instead of branches): transformed data is random, so branches would mispredict. */
 static inline uint64_t gadd(uint64_t a, uint64_t b) {
     uint64_t s = a + b;
-    if (s < a) return s + GEPS; /* wrapped past 2^64: add 2^64 mod p back; stays below p */
-    return s >= GP ? s - GP : s;
+    s += (0 - (uint64_t)(s < a)) & GEPS;     /* wrapped past 2^64: add 2^64 mod p back; stays below 2^64 */
+    return s - ((0 - (uint64_t)(s >= GP)) & GP);
 }
-static inline uint64_t gsub(uint64_t a, uint64_t b) { return a >= b ? a - b : a - b + GP; }
+static inline uint64_t gsub(uint64_t a, uint64_t b) { return a - b + ((0 - (uint64_t)(a < b)) & GP); }
 static inline uint64_t gred(unsigned __int128 x) {
     uint64_t lo = (uint64_t)x, hi = (uint64_t)(x >> 64);
     uint64_t hh = hi >> 32, hl = hi & GEPS;
-    uint64_t t = lo - hh;          /* lo + hl 2^64 + hh 2^96 = lo - hh + hl (2^32 - 1) */
-    if (lo < hh) t -= GEPS;        /* borrow: the wrapped value holds an extra 2^64 = 2^32 - 1 */
-    uint64_t u = hl * GEPS;        /* < 2^64 */
+    uint64_t t = lo - hh;                       /* lo + hl 2^64 + hh 2^96 = lo - hh + hl (2^32 - 1) */
+    t -= (0 - (uint64_t)(lo < hh)) & GEPS;      /* borrow: the wrapped value holds an extra 2^64 = 2^32 - 1 */
+    uint64_t u = hl * GEPS;                     /* < 2^64 */
     uint64_t r = t + u;
-    if (r < u) r += GEPS;          /* carry: 2^64 = 2^32 - 1 again; cannot wrap twice */
-    return r >= GP ? r - GP : r;
+    r += (0 - (uint64_t)(r < u)) & GEPS;        /* carry: 2^64 = 2^32 - 1 again; cannot wrap twice */
+    return r - ((0 - (uint64_t)(r >= GP)) & GP);
 }
 static inline uint64_t gmul(uint64_t a, uint64_t b) { return gred((unsigned __int128)a * b); }
 static uint64_t gpow(uint64_t a, uint64_t e) {
@@ -267,39 +268,65 @@ static const root_tables *roots(void) {
     return r;
 }
 
-/* One wide layer (butterfly span half = len/2 over the whole array), parallel over butterflies. */
-static void wide_layer(uint64_t *a, uint64_t L, uint64_t len, int inverse) {
-    const uint64_t half = len >> 1, w = groot(len, inverse), total = L >> 1;
+/* All wide layers (len > NTT_BLOCK) of one direction.  A wide butterfly pairs indices that differ by a
+ * multiple of NTT_BLOCK, so the wide layers act on each column of the L/NTT_BLOCK x NTT_BLOCK matrix
+ * view separately: a thread copies WIDE_COLS neighbouring columns (one cache line per row) into a buffer,
+ * runs every wide layer there and writes them back -- one pass over memory instead of one per layer.
+ * Butterfly k = q NTT_BLOCK + c (row q of its block, column c) has twiddle w_len^k = w_lr^q w_len^c with
+ * lr = len / NTT_BLOCK; the factors are formed once per layer, group and row q (not per block). */
+#define WIDE_COLS 8
+
+static void wide_layers(uint64_t *a, uint64_t L, int inverse) {
+    const uint64_t M = L / NTT_BLOCK; /* rows */
+    if (M < 2) return;
+    int nl = 0;
+    uint64_t wl[40], wr[40]; /* per layer: w_len, w_lr (inverse roots for the inverse transform) */
+    for (uint64_t len = 2 * NTT_BLOCK; len <= L; len <<= 1, ++nl) {
+        wl[nl] = groot(len, inverse);
+        wr[nl] = groot(len / NTT_BLOCK, inverse);
+    }
 #ifdef _OPENMP
 #pragma omp parallel
 #endif
     {
-        uint64_t nt = 1, id = 0;
+        uint64_t *buf = (uint64_t *)malloc(M * WIDE_COLS * 8);
 #ifdef _OPENMP
-        nt = (uint64_t)omp_get_num_threads();
-        id = (uint64_t)omp_get_thread_num();
+#pragma omp for schedule(static)
 #endif
-        uint64_t j0 = total * id / nt, j1 = total * (id + 1) / nt;
-        uint64_t k = j0 % half, s = (j0 / half) * len;
-        uint64_t wk = gpow(w, k);
-        for (uint64_t j = j0; j < j1; ++j) {
-            uint64_t *x = a + s + k, *y = x + half;
-            if (!inverse) { /* DIF: (u + v, (u - v) w^k) */
-                uint64_t u = *x, v = *y;
-                *x = gadd(u, v);
-                *y = gmul(gsub(u, v), wk);
-            } else { /* DIT: (u + v w^-k, u - v w^-k) */
-                uint64_t u = *x, v = gmul(*y, wk);
-                *x = gadd(u, v);
-                *y = gsub(u, v);
+        for (int64_t g = 0; g < (int64_t)(NTT_BLOCK / WIDE_COLS); ++g) {
+            const uint64_t c0 = (uint64_t)g * WIDE_COLS;
+            for (uint64_t r = 0; r < M; ++r)
+                for (int c = 0; c < WIDE_COLS; ++c) buf[r * WIDE_COLS + c] = a[r * NTT_BLOCK + c0 + c];
+            for (int li = 0; li < nl; ++li) {
+                /* DIF runs the layers from the widest down, DIT from the narrowest up */
+                const int l = inverse ? li : nl - 1 - li;
+                const uint64_t lr = 2ull << l, hr = lr >> 1; /* rows per block of this layer, half */
+                uint64_t tc[WIDE_COLS];
+                tc[0] = gpow(wl[l], c0);
+                for (int c = 1; c < WIDE_COLS; ++c) tc[c] = gmul(tc[c - 1], wl[l]);
+                /* row q of every block shares its twiddles: q outermost, so each is formed once */
+                for (uint64_t q = 0; q < hr; ++q) {
+                    for (uint64_t r0 = 0; r0 < M; r0 += lr) {
+                        uint64_t *x = buf + (r0 + q) * WIDE_COLS, *y = x + hr * WIDE_COLS;
+                        for (int c = 0; c < WIDE_COLS; ++c) {
+                            if (!inverse) {
+                                uint64_t u = x[c], v = y[c];
+                                x[c] = gadd(u, v);
+                                y[c] = gmul(gsub(u, v), tc[c]);
+                            } else {
+                                uint64_t u = x[c], v = gmul(y[c], tc[c]);
+                                x[c] = gadd(u, v);
+                                y[c] = gsub(u, v);
+                            }
+                        }
+                    }
+                    for (int c = 0; c < WIDE_COLS; ++c) tc[c] = gmul(tc[c], wr[l]);
+                }
             }
-            wk = gmul(wk, w);
-            if (++k == half) {
-                k = 0;
-                s += len;
-                wk = 1;
-            }
+            for (uint64_t r = 0; r < M; ++r)
+                for (int c = 0; c < WIDE_COLS; ++c) a[r * NTT_BLOCK + c0 + c] = buf[r * WIDE_COLS + c];
         }
+        free(buf);
     }
 }
 
@@ -339,7 +366,7 @@ static void narrow_layers(uint64_t *a, uint64_t L, int inverse) {
 
 /* Forward transform, natural order in, bit-reversed order out (decimation in frequency). */
 static void ntt_dif(uint64_t *a, uint64_t L) {
-    for (uint64_t len = L; len > NTT_BLOCK; len >>= 1) wide_layer(a, L, len, 0);
+    wide_layers(a, L, 0);
     narrow_layers(a, L, 0);
 }
 
@@ -347,7 +374,7 @@ static void ntt_dif(uint64_t *a, uint64_t L) {
  * time): ntt_dit(ntt_dif(x)) = L x. */
 static void ntt_dit(uint64_t *a, uint64_t L) {
     narrow_layers(a, L, 1);
-    for (uint64_t len = 2 * NTT_BLOCK; len <= L; len <<= 1) wide_layer(a, L, len, 1);
+    wide_layers(a, L, 1);
 }
 
 /* Transform length: n for power-of-two n (cyclic), else the next power of two >= n + h + 1 (a linear
@@ -406,13 +433,12 @@ void pa_oracle_ntt_seed_free(void *ctx) {
     free(c);
 }
 
-/* c[i] = sum_{j=0..h} key_start[j] * seed[(i-j) mod n] for i < count, exact, into conv (count values). */
-static int conv_with_seed(const ntt_seed *c, const uint32_t *key_start, uint64_t count, int64_t *conv) {
-    const uint64_t L = c->L, n = c->n, h = c->h;
-    const int pow2 = (c->n & (c->n - 1u)) == 0;
-    if (count > n) return -1;
+/* The exact linear (or, for power-of-two n, cyclic) convolution of key_start bits 0..h with the seed, in
+ * natural order: L values, freed by the caller.  Value i + n folds onto i for non-power-of-two n. */
+static uint64_t *conv_values(const ntt_seed *c, const uint32_t *key_start) {
+    const uint64_t L = c->L, h = c->h;
     uint64_t *A = (uint64_t *)malloc(L * 8);
-    if (!A) return -1;
+    if (!A) return NULL;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -423,6 +449,16 @@ static int conv_with_seed(const ntt_seed *c, const uint32_t *key_start, uint64_t
 #endif
     for (int64_t i = 0; i < (int64_t)L; ++i) A[i] = gmul(A[i], c->S[i]);
     ntt_dit(A, L);
+    return A;
+}
+
+/* c[i] = sum_{j=0..h} key_start[j] * seed[(i-j) mod n] for i < count, exact, into conv (count values). */
+static int conv_with_seed(const ntt_seed *c, const uint32_t *key_start, uint64_t count, int64_t *conv) {
+    const uint64_t L = c->L, n = c->n;
+    const int pow2 = (c->n & (c->n - 1u)) == 0;
+    if (count > n) return -1;
+    uint64_t *A = conv_values(c, key_start);
+    if (!A) return -1;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -448,11 +484,19 @@ int pa_oracle_conv_exact(const uint32_t *seed, const uint32_t *key_start, uint32
     return rc;
 }
 
-/* Output bytes from the exact convolution values: bit i = c[i] mod 2 (XOR key_rest bit i for i < v when
- * PA_FLAG_XOR_KEY_REST), byte i/8, bit 7 - i%8.  ob is a multiple of 8. */
-static void emit_parity(const int64_t *c, uint64_t ob, const uint32_t *key_rest, uint32_t v, uint32_t flags,
-                        uint8_t *out) {
-    const int x = (flags & PA_FLAG_XOR_KEY_REST) && key_rest;
+/* Full block with a prepared seed transform (pa_oracle_ntt_seed_prepare for the same n, v).  Output bit
+ * i = c[i] mod 2 (XOR key_rest bit i for i < v when PA_FLAG_XOR_KEY_REST) goes to byte i/8, bit
+ * 7 - i%8; the output length is a multiple of 8 bits. */
+int pa_oracle_ntt_with_seed(void *ctx, const uint32_t *key_start, const uint32_t *key_rest, uint32_t flags,
+                            uint8_t *out, int nthreads) {
+    ntt_seed *c = (ntt_seed *)ctx;
+    if (!c) return -1;
+    set_threads(nthreads);
+    const uint64_t ob = pa_oracle_out_bits(c->n, c->v, flags), L = c->L, n = c->n;
+    const int pow2 = (c->n & (c->n - 1u)) == 0, x = (flags & PA_FLAG_XOR_KEY_REST) && key_rest;
+    const uint32_t v = c->v;
+    uint64_t *A = conv_values(c, key_start);
+    if (!A) return -1;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -460,26 +504,14 @@ static void emit_parity(const int64_t *c, uint64_t ob, const uint32_t *key_rest,
         uint32_t byte = 0;
         for (uint32_t t = 0; t < 8; ++t) {
             uint64_t i = 8u * (uint64_t)b + t;
-            uint32_t bit = (uint32_t)(c[i] & 1);
+            uint32_t bit = (uint32_t)(A[i] & 1u);
+            if (!pow2 && i + n < L) bit ^= (uint32_t)(A[i + n] & 1u);
             if (x && i < v) bit ^= bit_msb(key_rest, i);
             byte |= bit << (7u - t);
         }
         out[b] = (uint8_t)byte;
     }
-}
-
-/* Full block with a prepared seed transform (pa_oracle_ntt_seed_prepare for the same n, v). */
-int pa_oracle_ntt_with_seed(void *ctx, const uint32_t *key_start, const uint32_t *key_rest, uint32_t flags,
-                            uint8_t *out, int nthreads) {
-    ntt_seed *c = (ntt_seed *)ctx;
-    if (!c) return -1;
-    set_threads(nthreads);
-    uint64_t ob = pa_oracle_out_bits(c->n, c->v, flags);
-    int64_t *conv = (int64_t *)malloc(ob * 8);
-    if (!conv) return -1;
-    if (conv_with_seed(c, key_start, ob, conv)) { free(conv); return -1; }
-    emit_parity(conv, ob, key_rest, c->v, flags, out);
-    free(conv);
+    free(A);
     return 0;
 }
 

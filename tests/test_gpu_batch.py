@@ -197,3 +197,38 @@ def test_pool_refuses_blocks_beyond_one_fp32_pass(torch_cuda, engine):
     with pytest.raises(pa.PAError) as ei:
         engine.submit(hjob)
     assert ei.value.code == pa.PA_ERR_TOO_LARGE
+
+
+def test_two_slots_concurrently_many_times(torch_cuda, engine):
+    """Two blocks of different sizes -- a power of two with a cached static seed, and a padded size with
+    its own seed -- run concurrently on two slots, 200 times over (streams, then graph replays), and each
+    result is compared with the oracle every time.  Slots share no mutable device state: each has its
+    own working set, error word and tensor maps; per-job counters and residual words are per job; the
+    cached spectrum is only read."""
+    dev = torch_cuda.device("cuda")
+    t = lambda a: torch_cuda.from_numpy(np.ascontiguousarray(a).view(np.int32)).to(dev)
+    na, va = 1 << 22, 3 << 19
+    nb, vb = 3 * (1 << 20) + 5 * 1024, 1234 * 128
+    seed_a, recv_a = O.random_block(na, va, 0xA11)
+    seed_b, recv_b = O.random_block(nb, vb, 0xB22)
+    ks_a, kr_a = O.key_split(recv_a, na, va)
+    ks_b, kr_b = O.key_split(recv_b, nb, vb)
+    want_a = O.ntt(seed_a, ks_a, kr_a, na, va, DEFAULT)
+    want_b = O.ntt(seed_b, ks_b, kr_b, nb, vb, pa.FLAG_COMPRESS)
+    sid = engine.seed_cache_add(seed_a, na, va)
+    engine.set_pool(0, 16, 2)
+    d = [t(x) for x in (ks_a, kr_a, seed_b, ks_b, kr_b)]
+    out_a = torch_cuda.zeros(va // 8, dtype=torch_cuda.uint8, device=dev)
+    out_b = torch_cuda.zeros(vb // 8, dtype=torch_cuda.uint8, device=dev)
+    jobs = [pa.PAJob(None, sid, d[0].data_ptr(), d[1].data_ptr(), na, va, DEFAULT, out_a.data_ptr()),
+            pa.PAJob(d[2].data_ptr(), -1, d[3].data_ptr(), d[4].data_ptr(), nb, vb, pa.FLAG_COMPRESS,
+                     out_b.data_ptr())]
+    for it in range(200):
+        out_a.fill_(it & 0xFF)
+        out_b.fill_(~it & 0xFF)
+        torch_cuda.cuda.synchronize()  # the fills run on torch's stream, the batch on the engine's
+        engine.batch_run(jobs, pa.BATCH_GRAPH if it >= 150 else 0)
+        st = engine.batch_sync(2)
+        assert st[0].exact == 0 and st[1].exact == 0
+        assert np.array_equal(out_a.cpu().numpy(), want_a), it
+        assert np.array_equal(out_b.cpu().numpy(), want_b), it

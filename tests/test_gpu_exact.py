@@ -2,7 +2,8 @@
 
 Precision-stress configuration: blocks whose FP32 rounding budget is exceeded (a seed with a long run of
 ones and an all-ones key) must still be bit-exact -- pa_process detects them by their residual and
-recomputes them exactly; n = 2^29 blocks (dynamic seed) run on the exact path only.
+recomputes them exactly.  Blocks beyond 2^27 bits (n = 2^29 with a fresh seed per block) run on the FP32
+path as 2^27-bit chunk blocks under the same guard, with the exact path as the fallback.
 """
 import numpy as np
 import pytest
