@@ -303,6 +303,13 @@ def spread(xs):
             "repeats": len(ys)}
 
 
+def rate_spread(seconds, to_rate):
+    """Spread of repeated timed regions as rates (min/max of the rate, not of the time)."""
+    out = spread([to_rate(t) for t in seconds])
+    out["median"] = to_rate(statistics.median(seconds))
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -510,16 +517,16 @@ def run_ours(args):
         "blocks_in_flight": IN_FLIGHT,
         "repeats": {"count": R, "what": "the K-step timed region is run R times (each bracketed by a sync); "
                                         "value = median repeat",
-                    "gbit_s": {k: (gbit(v) if k != "repeats" else v) for k, v in s_conc.items()}},
+                    "gbit_s": rate_spread(t_conc, gbit)},
         "e2e": {"value": gbit(s_e2e["median"]), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "api": "pa_submit/pa_poll, %d blocks in flight, pinned host buffers" % E2E_IN_FLIGHT,
-                "repeats_gbit_s": {k: (gbit(v) if k != "repeats" else v) for k, v in s_e2e.items()},
+                "repeats_gbit_s": rate_spread(t_e2e, gbit),
                 "output_equals_pa_process": same_out, "clocks": clk_e2e.summary(),
                 "sync_value": gbit(s_sync["median"]), "sync_api": "pa_process, one block at a time"},
         "gpu_launches": K * pa.kernels_per_block(N_BITS, V_BITS),
         "value_one_stream": {"value": gbit(s_one["median"]), "unit": UNIT,
-                             "repeats_gbit_s": {k: (gbit(v) if k != "repeats" else v) for k, v in s_one.items()},
+                             "repeats_gbit_s": rate_spread(t_one, gbit),
                              "api": "pa_process_device, one block after another on one stream",
                              "output_equals_in_flight": conc_equal, "clocks": clk_one.summary()},
         "latency_ms": {"device_p50": pct(blk_ms, 50), "device_p99": pct(blk_ms, 99), "device_max": max(blk_ms),
