@@ -174,8 +174,23 @@ PA_API int pa_seed_cache_clear(pa_engine* e);
  * exactly, and fills stats[i] for job i (gpu_ms: the whole batch's device time). */
 #define PA_BATCH_GRAPH 1u
 #define PA_BATCH_SERIAL 2u
+#define PA_BATCH_PERSISTENT 4u
 PA_API int pa_batch_run(pa_engine* e, const pa_job* jobs, uint32_t count, uint32_t batch_flags, void* stream);
 PA_API int pa_batch_sync(pa_engine* e, pa_stats* stats, uint32_t count);
+
+/* PA_BATCH_PERSISTENT: the whole batch runs as ONE persistent kernel launch (with PA_BATCH_GRAPH, that
+ * launch captured in a CUDA graph and replayed).  The launch holds one 512-thread CTA per SM, cut into
+ * lanes of ctas_per_lane CTAs; a lane takes one block at a time, longest first from a device-side list,
+ * and its CTAs run the block's passes between lane barriers (bounded waits: an expired one makes
+ * pa_batch_sync return PA_ERR_CUDA with cudaErrorLaunchTimeout).  Every block's arrays live in its
+ * lane's working set (about 12 * Np bytes, Np the largest cyclic length the lanes hold), so the number of
+ * lanes is what the pool's HBM budget admits.  Blocks run with rows of 2^14 and a cyclic length of at
+ * least 2^20 (a smaller block is placed in 2^20), up to n = 2^27.  Static seeds get a spectrum in the
+ * lanes' layout the first time a batch uses them.  pa_set_lanes sets the CTAs per lane (0 = 4) and
+ * sizes the lanes for cyclic lengths up to max_np (a power of two; 0 = the largest block of each batch);
+ * returns the number of lanes allocated (0 if none yet) or a negative PA_ERR_* code.  No counterpart
+ * in the reference (one block per mainloop pass, PrivacyAmplification.cu:1686-2118). */
+PA_API int pa_set_lanes(pa_engine* e, int32_t ctas_per_lane, uint32_t max_np);
 
 /* Served blocks with HOST pointers (pinned memory lets the copies overlap): pa_submit admits the
  * block to a free slot (creating one if the HBM budget allows), queues copy-in, kernels and copy-out,

@@ -31,6 +31,7 @@ PA_ERR_BUSY = -6
 PA_PENDING = 1
 BATCH_GRAPH = 1
 BATCH_SERIAL = 2
+BATCH_PERSISTENT = 4
 FLAG_XOR_KEY_REST = 1
 FLAG_COMPRESS = 2
 FLAG_EXACT = 4
@@ -41,7 +42,8 @@ EXPORTS = ("pa_create", "pa_destroy", "pa_set_seed", "pa_process", "pa_set_seed_
            "pa_sync", "pa_key_split", "pa_output_bytes", "pa_kernels_per_block", "pa_set_timing",
            "pa_stage_times", "pa_error_string", "pa_last_cuda_error", "pa_process_noalloc", "pa_set_pool",
            "pa_seed_cache_add", "pa_seed_cache_clear", "pa_batch_run", "pa_batch_sync", "pa_submit", "pa_poll",
-           "pa_set_split", "pa_get_split", "pa_autotune", "pa_pool_reserve", "pa_selftest_wait_timeout")
+           "pa_set_split", "pa_get_split", "pa_autotune", "pa_pool_reserve", "pa_selftest_wait_timeout",
+           "pa_set_lanes")
 
 
 class PAError(RuntimeError):
@@ -120,6 +122,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pa_get_split": ([eng, ctypes.c_uint32], ctypes.c_int),
         "pa_autotune": ([eng, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
         "pa_pool_reserve": ([eng, ctypes.c_uint32, ctypes.c_int32], ctypes.c_int),
+        "pa_set_lanes": ([eng, ctypes.c_int32, ctypes.c_uint32], ctypes.c_int),
         "pa_selftest_wait_timeout": ([ctypes.c_int32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
@@ -274,6 +277,14 @@ class Engine:
         rc = self._lib.pa_pool_reserve(self._h, max_np, count)
         if rc < 0:
             self._check(rc, "pa_pool_reserve")
+        return rc
+
+    def set_lanes(self, ctas_per_lane: int = 0, max_np: int = 0) -> int:
+        """Persistent lanes (PA_BATCH_PERSISTENT): CTAs per lane and the largest cyclic length they hold;
+        returns the number of lanes allocated (0 until the first persistent batch when max_np is 0)."""
+        rc = self._lib.pa_set_lanes(self._h, ctas_per_lane, max_np)
+        if rc < 0:
+            self._check(rc, "pa_set_lanes")
         return rc
 
     def seed_cache_add(self, seed_words, n: int, v: int, flags: int = DEFAULT_FLAGS) -> int:

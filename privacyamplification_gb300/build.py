@@ -16,12 +16,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpa_gb300.so")
-SOURCES = ["pa_kernels.cu", "pa_passes.cu", "pa_ntt.cu", "pa_chunk.cu", "pa_engine.cu", "pa_batch.cu", "pa_noalloc.cu", "pa_selftest.cu"]
+SOURCES = ["pa_kernels.cu", "pa_passes.cu", "pa_lanes.cu", "pa_ntt.cu", "pa_chunk.cu", "pa_engine.cu", "pa_batch.cu",
+           "pa_noalloc.cu", "pa_selftest.cu"]
 HOST_SOURCES = ["pa_sha3.cpp", "pa_config.cpp", "pa_zmtp.cpp", "pa_service.cpp"]  # plain C++, no CUDA
 SERVICE_MAIN = "pa_service_main.cpp"
 SERVICE = os.path.join(HERE, "pa_service")
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall"]
-HEADERS = ["pa_device.cuh", "pa_fft.cuh", "pa_tma.cuh", "pa_kernels.cuh", "pa_engine_impl.h",
+HEADERS = ["pa_device.cuh", "pa_fft.cuh", "pa_tma.cuh", "pa_kernels.cuh", "pa_pass_bodies.cuh", "pa_lanes.cuh", "pa_engine_impl.h",
            os.path.join("..", "..", "include", "pa_gb300.h"), os.path.join("..", "..", "include", "pa_service.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",

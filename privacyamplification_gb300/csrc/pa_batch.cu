@@ -1,15 +1,19 @@
 // pa_batch.cu -- many blocks on one GPU: a pool of slots (one CUDA stream + working set each), the
-// static-seed spectrum cache, batched runs (optionally one CUDA graph per batch), served blocks
-// (pa_submit / pa_poll, admission by free slot and HBM budget) and the three-pass split autotuner.
+// static-seed spectrum cache, batched runs (optionally one CUDA graph per batch, or one persistent lane
+// launch, pa_lanes.cuh), served blocks (pa_submit / pa_poll, admission by free slot and HBM budget) and
+// the three-pass split autotuner.
 //
 // The reference has none of this (one block at a time, PrivacyAmplification.cu:1686-2118); the
 // per-block work is the same key-block / seed-spectrum kernels the single-block engine runs.
 #include "pa_engine_impl.h"
+#include "pa_lanes.cuh"
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstring>
+#include <map>
 #include <new>
 #include <numeric>
 #include <unordered_map>
@@ -66,6 +70,36 @@ struct Slot {
     uint64_t last_use = 0;
 };
 
+// A static seed's spectrum in the lane layout (pa_lanes.cuh).
+struct LaneSpec {
+    float2* spec = nullptr;
+    unsigned long long* cnt = nullptr;  // [0] unused, [1] popcount of the placed seed, then a scratch word
+    size_t bytes = 0;
+};
+
+// A captured persistent launch and the job array it reads.
+struct LaneGraph {
+    cudaGraphExec_t exec = nullptr;
+    pa::LaneJob* jobs = nullptr;
+};
+
+// The persistent lane engine's working sets: `lanes` lanes of T CTAs, each with a block's arrays for
+// cyclic lengths up to 2^cap.
+struct LaneSet {
+    int T = 0, lanes = 0, cap = 0;
+    size_t bytes = 0, smem = 0;
+    float2 *work = nullptr, *work2 = nullptr, *spec = nullptr;
+    uint32_t* planes = nullptr;
+    size_t work_stride = 0, planes_stride = 0;
+    CUtensorMap* maps = nullptr;   // [lane][log_n1][Y, Z]
+    unsigned int* ctl = nullptr;   // next, bar[lanes], slot[lanes], err[lanes]
+    pa::LaneJob* jobs = nullptr;   // uncaptured launches
+    uint32_t job_cap = 0;
+    int early_b[pa::kLaneMaps] = {}, early_c[pa::kLaneMaps] = {};
+    std::map<std::array<uint64_t, 4>, LaneSpec> spectra;
+    std::unordered_map<uint64_t, LaneGraph> graphs;
+};
+
 struct Pool {
     std::vector<Slot*> slots;
     std::vector<SeedEntry> seeds;
@@ -86,6 +120,11 @@ struct Pool {
     cudaStream_t batch_stream = nullptr;
     bool batch_pending = false;
     std::unordered_map<uint64_t, cudaGraphExec_t> graphs;
+    // persistent lane launches
+    LaneSet* lanes = nullptr;
+    int lane_ctas = 4;        // CTAs per lane (pa_set_lanes)
+    int lane_cap = 0;         // log2 of the cyclic length the lanes are sized for (0: the batch's largest)
+    bool batch_lanes = false; // the pending batch ran on the lanes
 };
 
 namespace {
@@ -172,9 +211,41 @@ Pool* get_pool(pa_engine* e) {
     return p;
 }
 
+void drop_lane_graphs(LaneSet* ls) {
+    if (!ls) return;
+    for (auto& kv : ls->graphs) {
+        cudaGraphExecDestroy(kv.second.exec);
+        cudaFree(kv.second.jobs);
+    }
+    ls->graphs.clear();
+}
+
 void drop_graphs(Pool* p) {
     for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second);
     p->graphs.clear();
+    drop_lane_graphs(p->lanes);
+}
+
+void free_lanes(Pool* p) {
+    LaneSet* ls = p->lanes;
+    if (!ls) return;
+    cudaDeviceSynchronize();
+    drop_lane_graphs(ls);
+    cudaFree(ls->work);
+    cudaFree(ls->work2);
+    cudaFree(ls->spec);
+    cudaFree(ls->planes);
+    cudaFree(ls->maps);
+    cudaFree(ls->ctl);
+    cudaFree(ls->jobs);
+    for (auto& kv : ls->spectra) {
+        cudaFree(kv.second.spec);
+        cudaFree(kv.second.cnt);
+        p->used -= std::min(p->used, kv.second.bytes);
+    }
+    p->used -= std::min(p->used, ls->bytes);
+    delete ls;
+    p->lanes = nullptr;
 }
 
 int ensure_slot_maps(pa_engine* e, Slot* sl, const BlockGeom& g) {
@@ -299,12 +370,285 @@ int batch_enqueue(pa_engine* e, Pool* p, const std::vector<std::vector<int>>& or
     return PA_OK;
 }
 
+// Per-job popcount and residual words for `count` jobs.
+int ensure_job_arrays(pa_engine* e, Pool* p, uint32_t count) {
+    if (p->job_cap >= count) return PA_OK;
+    cudaFree(p->job_cnt);
+    cudaFree(p->job_resid);
+    p->job_cnt = nullptr;
+    p->job_resid = nullptr;
+    p->job_cap = 0;
+    drop_graphs(p);
+    PA_CUDA(e, cudaMalloc(&p->job_cnt, (size_t)count * 2 * sizeof(unsigned long long)));
+    PA_CUDA(e, cudaMalloc(&p->job_resid, (size_t)count * sizeof(unsigned int)));
+    p->job_cap = count;
+    return PA_OK;
+}
+
+// ---------------------------------------------------------------------------------------- lanes
+// Block geometry on the lanes: rows of 2^14, the cyclic length at least 2^20 (pa_lanes.cuh).
+int lane_geom(uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
+    if (n < 1024u || (n & 31u) || (v & 31u) || v == 0 || v >= n) return PA_ERR_INVALID_ARG;
+    g->n = n;
+    g->v = v;
+    g->h = n - v;
+    g->out_bits = (flags & PA_FLAG_COMPRESS) ? v : n / 2u;
+    const uint64_t need = is_pow2(n) ? n : std::max<uint64_t>(n, (uint64_t)g->out_bits + g->h);
+    g->log_np = std::max(ceil_log2(need), pa::kLaneMinLogNp);
+    if (g->log_np > pa::kLaneMaxLogNp) return PA_ERR_TOO_LARGE;
+    const uint64_t np = 1ull << g->log_np;
+    g->seed_direct = np == n ? n : (uint32_t)std::min<uint64_t>(np - g->h, n);
+    g->log_n = g->log_np - 1;
+    g->log_n2 = pa::kLaneLogRow;
+    g->log_n1 = g->log_n - pa::kLaneLogRow;
+    g->exact_only = 0;
+    return PA_OK;
+}
+
+size_t lane_bytes(int cap) {
+    const size_t np = size_t(1) << cap;
+    return 3 * (np / 2) * sizeof(float2) + np / 8 + 256;
+}
+
+// Lanes of p->lane_ctas CTAs for cyclic lengths up to 2^cap: as many as fit the resident CTAs of the
+// lane kernel and the HBM budget.
+int ensure_lanes(pa_engine* e, Pool* p, int cap) {
+    cap = std::max(cap, p->lane_cap);
+    LaneSet* ls = p->lanes;
+    if (ls && ls->cap >= cap && ls->T == p->lane_ctas) return PA_OK;
+    free_lanes(p);
+    int ctas = 0;
+    int rc = pa::lane_max_ctas(&ctas);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    const int T = p->lane_ctas;
+    int lanes = ctas / T;
+    const size_t per = lane_bytes(cap);
+    while (lanes > 0 && p->used + (size_t)lanes * per > p->budget) --lanes;
+    if (lanes == 0) return PA_ERR_TOO_LARGE;
+    ls = new (std::nothrow) LaneSet();
+    if (!ls) return PA_ERR_INVALID_ARG;
+    ls->T = T;
+    ls->lanes = lanes;
+    ls->cap = cap;
+    ls->smem = pa::lane_smem_bytes();
+    const size_t np = size_t(1) << cap;
+    ls->work_stride = np / 2;
+    ls->planes_stride = np / 32 + 64;
+    cudaError_t err = cudaSuccess;
+    auto A = [&](void** ptr, size_t bytes) {
+        if (err == cudaSuccess) err = cudaMalloc(ptr, bytes);
+    };
+    A((void**)&ls->work, (size_t)lanes * ls->work_stride * sizeof(float2));
+    A((void**)&ls->work2, (size_t)lanes * ls->work_stride * sizeof(float2));
+    A((void**)&ls->spec, (size_t)lanes * ls->work_stride * sizeof(float2));
+    A((void**)&ls->planes, (size_t)lanes * ls->planes_stride * sizeof(uint32_t));
+    A((void**)&ls->maps, (size_t)lanes * pa::kLaneMaps * 2 * sizeof(CUtensorMap));
+    A((void**)&ls->ctl, (1 + 3 * (size_t)lanes) * sizeof(unsigned int));
+    ls->bytes = (size_t)lanes * per;
+    p->used += ls->bytes;
+    p->lanes = ls;
+    if (err != cudaSuccess) {
+        free_lanes(p);
+        return cuda_fail(e, err);
+    }
+    std::vector<CUtensorMap> maps((size_t)lanes * pa::kLaneMaps * 2);
+    for (int l = 0; l < lanes; ++l) {
+        rc = pa::make_lane_maps(ls->work + (size_t)l * ls->work_stride, ls->work2 + (size_t)l * ls->work_stride,
+                                maps.data() + (size_t)l * pa::kLaneMaps * 2);
+        if (rc) {
+            free_lanes(p);
+            return cuda_fail(e, (cudaError_t)rc);
+        }
+    }
+    err = cudaMemcpy(ls->maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) {
+        free_lanes(p);
+        return cuda_fail(e, err);
+    }
+    for (int i = 0; i < pa::kLaneMaps; ++i) {
+        ls->early_b[i] = pa::lane_early_boxes(pa::kLaneMinLogN1 + i, 'b', ls->smem);
+        ls->early_c[i] = pa::lane_early_boxes(pa::kLaneMinLogN1 + i, 'c', ls->smem);
+    }
+    return PA_OK;
+}
+
+// Key of a static seed's lane spectrum: the seed and its placement (any v shares the spectrum of a
+// power-of-two n that fills the cyclic length).
+std::array<uint64_t, 4> lane_spec_key(int32_t seed_id, const BlockGeom& g) {
+    const bool identity = (1ull << g.log_np) == g.n;
+    return {(uint64_t)seed_id, (uint64_t)g.log_np, identity ? 0ull : g.seed_direct, identity ? 0ull : g.h};
+}
+
+pa::LaneArgs lane_args(const LaneSet* ls, const pa::LaneJob* jobs, uint32_t njobs) {
+    pa::LaneArgs a{};
+    a.jobs = jobs;
+    a.njobs = njobs;
+    a.next = ls->ctl;
+    a.bar = ls->ctl + 1;
+    a.slot = reinterpret_cast<int*>(ls->ctl + 1 + ls->lanes);
+    a.err = reinterpret_cast<int*>(ls->ctl + 1 + 2 * ls->lanes);
+    a.work = ls->work;
+    a.work2 = ls->work2;
+    a.spec = ls->spec;
+    a.planes = ls->planes;
+    a.work_stride = ls->work_stride;
+    a.planes_stride = ls->planes_stride;
+    a.maps = ls->maps;
+    a.T = ls->T;
+    a.lanes = ls->lanes;
+    for (int i = 0; i < pa::kLaneMaps; ++i) {
+        a.early_b[i] = ls->early_b[i];
+        a.early_c[i] = ls->early_c[i];
+    }
+    a.wait_limit = 1u << 24;  // polls of ~0.1-1 us: seconds, far beyond any stage of a 2^27 block
+    return a;
+}
+
+// Queues one lane launch over `jobs` (uploaded to the lane set's job array).
+int lanes_launch(pa_engine* e, LaneSet* ls, const std::vector<pa::LaneJob>& jobs, cudaStream_t s) {
+    if (ls->job_cap < jobs.size()) {
+        cudaFree(ls->jobs);
+        ls->jobs = nullptr;
+        ls->job_cap = 0;
+        PA_CUDA(e, cudaMalloc(&ls->jobs, jobs.size() * sizeof(pa::LaneJob)));
+        ls->job_cap = (uint32_t)jobs.size();
+    }
+    PA_CUDA(e, cudaMemcpyAsync(ls->jobs, jobs.data(), jobs.size() * sizeof(pa::LaneJob), cudaMemcpyHostToDevice, s));
+    PA_CUDA(e, cudaMemsetAsync(ls->ctl, 0, (1 + 3 * (size_t)ls->lanes) * sizeof(unsigned int), s));
+    const pa::LaneArgs a = lane_args(ls, ls->jobs, (uint32_t)jobs.size());
+    int rc = pa::launch_lanes(a, ls->lanes * ls->T, ls->smem, s);
+    return rc ? cuda_fail(e, (cudaError_t)rc) : PA_OK;
+}
+
+// The batch on the lanes: lane spectra of new static seeds first (one launch), then the blocks, longest
+// first (one launch, or its captured graph with PA_BATCH_GRAPH).
+int lanes_batch(pa_engine* e, Pool* p, const pa_job* jobs, uint32_t count, uint32_t batch_flags, cudaStream_t s) {
+    std::vector<BlockGeom> lg(count);
+    int cap = pa::kLaneMinLogNp;
+    for (uint32_t i = 0; i < count; ++i) {
+        int rc = lane_geom(jobs[i].n, jobs[i].v, jobs[i].flags, &lg[i]);
+        if (rc) return rc;
+        cap = std::max(cap, lg[i].log_np);
+    }
+    int rc = ensure_lanes(e, p, cap);
+    if (rc) return rc;
+    LaneSet* ls = p->lanes;
+    std::vector<pa::LaneJob> builds;
+    for (uint32_t i = 0; i < count; ++i) {
+        if (jobs[i].seed_id < 0) continue;
+        const auto key = lane_spec_key(jobs[i].seed_id, lg[i]);
+        if (ls->spectra.count(key)) continue;
+        LaneSpec sp;
+        sp.bytes = (size_t(1) << lg[i].log_n) * sizeof(float2) + 32;
+        if (p->used + sp.bytes > p->budget) return PA_ERR_TOO_LARGE;
+        cudaError_t err = cudaMalloc(&sp.spec, (size_t(1) << lg[i].log_n) * sizeof(float2));
+        if (err == cudaSuccess) err = cudaMalloc(&sp.cnt, 4 * sizeof(unsigned long long));
+        if (err != cudaSuccess) {
+            cudaFree(sp.spec);
+            return cuda_fail(e, err);
+        }
+        p->used += sp.bytes;
+        ls->spectra[key] = sp;
+        pa::LaneJob b{};
+        b.seed = p->seeds[jobs[i].seed_id].seed;
+        b.spec_out = sp.spec;
+        b.cnt = sp.cnt;
+        b.resid = reinterpret_cast<unsigned int*>(sp.cnt + 2);
+        b.g = lg[i];
+        builds.push_back(b);
+    }
+    if (!builds.empty()) {
+        drop_lane_graphs(ls);
+        rc = lanes_launch(e, ls, builds, s);
+        if (rc) return rc;
+    }
+    std::vector<int> idx(count);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::vector<double> cost(count);
+    for (uint32_t i = 0; i < count; ++i) cost[i] = job_cost(lg[i], jobs[i].seed_id < 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<pa::LaneJob> lj(count);
+    for (uint32_t k = 0; k < count; ++k) {
+        const int i = idx[k];
+        const pa_job& jb = jobs[i];
+        pa::LaneJob& j = lj[k];
+        j.key_start = jb.key_start;
+        j.key_rest = (jb.flags & PA_FLAG_XOR_KEY_REST) ? jb.key_rest : nullptr;
+        if (jb.seed_id >= 0) {
+            const LaneSpec& sp = ls->spectra[lane_spec_key(jb.seed_id, lg[i])];
+            j.spec = sp.spec;
+            j.seed_cnt = sp.cnt + 1;
+        } else {
+            j.seed = jb.seed_words;
+        }
+        j.out = reinterpret_cast<uint32_t*>(jb.out);
+        j.cnt = p->job_cnt + 2 * (size_t)i;
+        j.resid = p->job_resid + i;
+        j.g = lg[i];
+        j.flags = jb.flags;
+    }
+    PA_CUDA(e, cudaEventRecord(p->b0, s));
+    if (batch_flags & PA_BATCH_GRAPH) {
+        uint64_t key = fnv(1469598103934665603ull, lj.data(), lj.size() * sizeof(pa::LaneJob));
+        auto it = ls->graphs.find(key);
+        if (it == ls->graphs.end()) {
+            LaneGraph lgph;
+            PA_CUDA(e, cudaMalloc(&lgph.jobs, lj.size() * sizeof(pa::LaneJob)));
+            PA_CUDA(e, cudaMemcpy(lgph.jobs, lj.data(), lj.size() * sizeof(pa::LaneJob), cudaMemcpyHostToDevice));
+            PA_CUDA(e, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+            cudaError_t cerr = cudaMemsetAsync(ls->ctl, 0, (1 + 3 * (size_t)ls->lanes) * sizeof(unsigned int), s);
+            int lrc = cerr == cudaSuccess
+                          ? pa::launch_lanes(lane_args(ls, lgph.jobs, count), ls->lanes * ls->T, ls->smem, s)
+                          : (int)cerr;
+            cudaGraph_t graph = nullptr;
+            cerr = cudaStreamEndCapture(s, &graph);
+            if (lrc || cerr != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                cudaFree(lgph.jobs);
+                return cuda_fail(e, lrc ? (cudaError_t)lrc : cerr);
+            }
+            cerr = cudaGraphInstantiate(&lgph.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (cerr != cudaSuccess) {
+                cudaFree(lgph.jobs);
+                return cuda_fail(e, cerr);
+            }
+            if (ls->graphs.size() >= 16) drop_lane_graphs(ls);
+            it = ls->graphs.emplace(key, lgph).first;
+        }
+        PA_CUDA(e, cudaGraphLaunch(it->second.exec, s));
+    } else {
+        rc = lanes_launch(e, ls, lj, s);
+        if (rc) return rc;
+    }
+    PA_CUDA(e, cudaEventRecord(p->b1, s));
+    return PA_OK;
+}
+
+// A slot for an exact recompute of a block of cyclic length 2^cap (one is made if none is idle).
+int exact_slot(pa_engine* e, Pool* p, int cap, Slot** out) {
+    for (Slot* c : p->slots)
+        if (!c->busy && c->cap >= cap) {
+            *out = c;
+            return PA_OK;
+        }
+    if (!make_room(p, slot_bytes(cap))) return PA_ERR_TOO_LARGE;
+    Slot* sl = nullptr;
+    int rc = new_slot(e, p, cap, &sl);
+    if (rc) return rc;
+    sl->last_use = ++p->clock;
+    p->slots.push_back(sl);
+    *out = sl;
+    return PA_OK;
+}
+
 }  // namespace
 
 void pool_destroy(pa_engine* e) {
     Pool* p = e->pool;
     if (!p) return;
     drop_graphs(p);
+    free_lanes(p);
     for (Slot* sl : p->slots) free_slot(p, sl);
     for (auto& se : p->seeds) {
         cudaFree(se.spec);
@@ -336,6 +680,26 @@ int pa_set_pool(pa_engine* e, uint64_t hbm_budget_bytes, int32_t max_slots, int3
     p->batch_slots = batch_slots ? batch_slots : 8;
     drop_graphs(p);
     return PA_OK;
+}
+
+int pa_set_lanes(pa_engine* e, int32_t ctas_per_lane, uint32_t max_np) {
+    if (!e || ctas_per_lane < 0 || ctas_per_lane > 1024) return PA_ERR_INVALID_ARG;
+    if (max_np && (max_np & (max_np - 1u))) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    Pool* p = get_pool(e);
+    if (!p) return PA_ERR_CUDA;
+    if (p->batch_pending) return PA_ERR_BUSY;
+    const int cap = max_np ? ceil_log2(max_np) : 0;
+    if (cap > pa::kLaneMaxLogNp) return PA_ERR_TOO_LARGE;
+    const int T = ctas_per_lane ? ctas_per_lane : 4;
+    if (p->lanes && (p->lanes->T != T || p->lanes->cap < cap)) free_lanes(p);
+    p->lane_ctas = T;
+    p->lane_cap = cap;
+    if (cap) {
+        int rc = ensure_lanes(e, p, cap);
+        if (rc) return rc;
+    }
+    return p->lanes ? p->lanes->lanes : 0;
 }
 
 int pa_pool_reserve(pa_engine* e, uint32_t max_np, int32_t count) {
@@ -466,6 +830,15 @@ int pa_batch_run(pa_engine* e, const pa_job* jobs, uint32_t count, uint32_t batc
         p->batch_pending = true;
         return PA_OK;
     }
+    if (batch_flags & PA_BATCH_PERSISTENT) {
+        int rc = ensure_job_arrays(e, p, count);
+        if (!rc) rc = lanes_batch(e, p, jobs, count, batch_flags, s);
+        if (rc) return rc;
+        p->batch_lanes = true;
+        p->batch_pending = true;
+        return PA_OK;
+    }
+    p->batch_lanes = false;
     int K = (batch_flags & PA_BATCH_SERIAL) ? 1 : std::min<int>(p->batch_slots, (int)count);
     K = std::min(K, p->max_slots);
     // slots 0..K-1 must hold the largest block of the batch
@@ -494,16 +867,9 @@ int pa_batch_run(pa_engine* e, const pa_job* jobs, uint32_t count, uint32_t batc
         if (rc) return rc;
         p->slots.insert(p->slots.begin() + k, sl);
     }
-    if (p->job_cap < count) {
-        cudaFree(p->job_cnt);
-        cudaFree(p->job_resid);
-        p->job_cnt = nullptr;
-        p->job_resid = nullptr;
-        p->job_cap = 0;
-        drop_graphs(p);
-        PA_CUDA(e, cudaMalloc(&p->job_cnt, (size_t)count * 2 * sizeof(unsigned long long)));
-        PA_CUDA(e, cudaMalloc(&p->job_resid, (size_t)count * sizeof(unsigned int)));
-        p->job_cap = count;
+    {
+        int rc = ensure_job_arrays(e, p, count);
+        if (rc) return rc;
     }
     // longest job first onto the least-loaded slot
     std::vector<int> idx(count);
@@ -575,6 +941,16 @@ int pa_batch_sync(pa_engine* e, pa_stats* stats, uint32_t count) {
             return PA_ERR_CUDA;
         }
     }
+    if (p->batch_lanes && p->lanes) {  // lane error words: an expired lane barrier or TMA wait
+        std::vector<int> lerr(p->lanes->lanes);
+        PA_CUDA(e, cudaMemcpy(lerr.data(), p->lanes->ctl + 1 + 2 * p->lanes->lanes, lerr.size() * sizeof(int),
+                              cudaMemcpyDeviceToHost));
+        for (int x : lerr)
+            if (x) {
+                e->last_cuda = (int)cudaErrorLaunchTimeout;
+                return PA_ERR_CUDA;
+            }
+    }
     if (nj == 0) return PA_OK;
     std::vector<unsigned long long> cnt(2 * (size_t)nj);
     std::vector<unsigned int> rb(nj);
@@ -587,8 +963,10 @@ int pa_batch_sync(pa_engine* e, pa_stats* stats, uint32_t count) {
         if (!(r <= e->residual_limit)) {  // FP32 budget exceeded: recompute this block exactly
             const pa_job& jb = p->jobs[j];
             const uint32_t* seed = jb.seed_id >= 0 ? p->seeds[jb.seed_id].seed : jb.seed_words;
-            Slot* sl = p->slots[0];
-            int rc = exact_in_slot(e, sl, p->geoms[j], seed, jb.key_start, jb.key_rest, jb.flags,
+            Slot* sl = nullptr;
+            int rc = exact_slot(e, p, p->geoms[j].log_np, &sl);
+            if (!rc)
+                rc = exact_in_slot(e, sl, p->geoms[j], seed, jb.key_start, jb.key_rest, jb.flags,
                                    reinterpret_cast<uint32_t*>(jb.out), sl->s);
             if (rc) return rc;
             PA_CUDA(e, cudaStreamSynchronize(sl->s));

@@ -71,6 +71,8 @@ struct PassMaps {
     CUtensorMap z;  // Z (pass B output, tile-major) as read by pass C
 };
 int make_pass_maps(const BlockGeom& g, const float2* Y, const float2* Z, PassMaps* out);
+// The Y and Z maps (out[0], out[1]) for columns of 2^log_n1, rows of 2^log_n2, pass B tiles of cpt columns.
+int encode_pass_maps(int log_n1, int log_n2, uint32_t cpt, const float2* Y, const float2* Z, CUtensorMap* out);
 int launch_pass_b(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y, float2* Z, float2* spec, int* err,
                   int num_sms, cudaStream_t s);
 int launch_pass_c(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
