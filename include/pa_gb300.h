@@ -192,6 +192,27 @@ PA_API int pa_batch_sync(pa_engine* e, pa_stats* stats, uint32_t count);
  * in the reference (one block per mainloop pass, PrivacyAmplification.cu:1686-2118). */
 PA_API int pa_set_lanes(pa_engine* e, int32_t ctas_per_lane, uint32_t max_np);
 
+/* Device-resident serving loop.  pa_serve_start launches the lane kernel in serving mode: its lanes
+ * (ctas_per_lane CTAs each, 0 = 38, i.e. four lanes on 152 SMs; as many as the HBM budget admits for
+ * cyclic lengths up to max_np, a power of two) poll a ring of ring_slots request slots (0 = 64) in pinned
+ * host memory.  A lane takes the next published request, runs it -- reading the request's inputs from
+ * host memory and writing its output there directly -- and publishes its completion; requests that
+ * arrive while others run are taken by the next free lane, so they overlap on the device.  The host only
+ * writes descriptors and reads completions: no launch or copy per request.  pa_serve_submit publishes a
+ * request (job pointers: pinned host or device memory -- pageable memory is refused with
+ * PA_ERR_INVALID_ARG; out holds pa_output_bytes() rounded up to a multiple of 4; a static seed_id needs its
+ * spectrum cached with pa_seed_cache_add before pa_serve_start) and returns its ticket, PA_ERR_BUSY when
+ * every ring slot holds a request not yet collected, PA_ERR_TOO_LARGE beyond max_np.  pa_serve_poll
+ * returns PA_PENDING, or PA_OK once job->out holds the result (a block over the residual limit is first
+ * recomputed exactly); the ring slot is then free.  The loop ends by itself after about two idle seconds
+ * and is started again by the next submit; pa_serve_stop ends it (after the requests it has taken) and
+ * frees the ring.  While serving, persistent batches return PA_ERR_BUSY.  The reference's counterpart is
+ * its host loop over ring slots with spin-waits (PrivacyAmplification.cu:1781-1797, 1990-1992). */
+PA_API int pa_serve_start(pa_engine* e, int32_t ctas_per_lane, uint32_t max_np, int32_t ring_slots);
+PA_API int pa_serve_submit(pa_engine* e, const pa_job* job, uint64_t* ticket);
+PA_API int pa_serve_poll(pa_engine* e, uint64_t ticket, pa_stats* stats);
+PA_API int pa_serve_stop(pa_engine* e);
+
 /* Served blocks with HOST pointers (pinned memory lets the copies overlap): pa_submit admits the
  * block to a free slot (creating one if the HBM budget allows), queues copy-in, kernels and copy-out,
  * and returns a ticket; PA_ERR_BUSY when nothing is free.  pa_poll returns PA_PENDING while the block

@@ -43,7 +43,7 @@ EXPORTS = ("pa_create", "pa_destroy", "pa_set_seed", "pa_process", "pa_set_seed_
            "pa_stage_times", "pa_error_string", "pa_last_cuda_error", "pa_process_noalloc", "pa_set_pool",
            "pa_seed_cache_add", "pa_seed_cache_clear", "pa_batch_run", "pa_batch_sync", "pa_submit", "pa_poll",
            "pa_set_split", "pa_get_split", "pa_autotune", "pa_pool_reserve", "pa_selftest_wait_timeout",
-           "pa_set_lanes")
+           "pa_set_lanes", "pa_serve_start", "pa_serve_submit", "pa_serve_poll", "pa_serve_stop")
 
 
 class PAError(RuntimeError):
@@ -123,6 +123,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pa_autotune": ([eng, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
         "pa_pool_reserve": ([eng, ctypes.c_uint32, ctypes.c_int32], ctypes.c_int),
         "pa_set_lanes": ([eng, ctypes.c_int32, ctypes.c_uint32], ctypes.c_int),
+        "pa_serve_start": ([eng, ctypes.c_int32, ctypes.c_uint32, ctypes.c_int32], ctypes.c_int),
+        "pa_serve_submit": ([eng, ctypes.POINTER(PAJob), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+        "pa_serve_poll": ([eng, ctypes.c_uint64, ctypes.POINTER(PAStats)], ctypes.c_int),
+        "pa_serve_stop": ([eng], ctypes.c_int),
         "pa_selftest_wait_timeout": ([ctypes.c_int32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
@@ -286,6 +290,35 @@ class Engine:
         if rc < 0:
             self._check(rc, "pa_set_lanes")
         return rc
+
+    # ---- device-resident serving loop -----------------------------------------------------------------
+    def serve_start(self, ctas_per_lane: int = 0, max_np: int = 1 << 27, ring_slots: int = 0) -> int:
+        """Starts the serving loop on the device; returns the number of lanes."""
+        rc = self._lib.pa_serve_start(self._h, ctas_per_lane, max_np, ring_slots)
+        if rc < 0:
+            self._check(rc, "pa_serve_start")
+        return rc
+
+    def serve_submit(self, job: PAJob):
+        """Publishes a request (host buffers pinned); returns its ticket, or None when the ring is full."""
+        t = ctypes.c_uint64()
+        rc = self._lib.pa_serve_submit(self._h, ctypes.byref(job), ctypes.byref(t))
+        if rc == PA_ERR_BUSY:
+            return None
+        self._check(rc, "pa_serve_submit")
+        return t.value
+
+    def serve_poll(self, ticket: int):
+        """None while the request runs, then its PAStats (job.out holds the result)."""
+        st = PAStats()
+        rc = self._lib.pa_serve_poll(self._h, ticket, ctypes.byref(st))
+        if rc == PA_PENDING:
+            return None
+        self._check(rc, "pa_serve_poll")
+        return st
+
+    def serve_stop(self):
+        self._check(self._lib.pa_serve_stop(self._h), "pa_serve_stop")
 
     def seed_cache_add(self, seed_words, n: int, v: int, flags: int = DEFAULT_FLAGS) -> int:
         s = _u32(seed_words)

@@ -100,6 +100,27 @@ struct LaneSet {
     std::unordered_map<uint64_t, LaneGraph> graphs;
 };
 
+// The device-resident serving loop (pa_serve_*): the lane kernel in serving mode, fed from a ring of
+// request slots in pinned host memory.
+struct ServeLoop {
+    pa::ServeSlot* ring = nullptr;  // pinned host memory
+    pa::ServeCtl* ctl = nullptr;    // pinned host memory
+    pa::ServeSlot* d_ring = nullptr;  // the same memory as the device addresses it
+    pa::ServeCtl* d_ctl = nullptr;
+    uint32_t size = 0;
+    unsigned long long* claimed = nullptr;  // device
+    pa::LaneJob* lane_job = nullptr;        // device
+    unsigned long long* lane_stats = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t ended = nullptr;  // recorded after each launch of the loop
+    bool launched = false;
+    uint64_t next_ticket = 0;
+    std::vector<uint64_t> owner;  // per ring slot: the ticket in it, or ~0 when free
+    std::vector<pa_job> jobs;     // per ring slot: the request as submitted (exact recompute)
+    std::vector<BlockGeom> geoms;
+    unsigned long long idle_ns = 2000000000ull;  // the loop ends after two seconds without requests
+};
+
 struct Pool {
     std::vector<Slot*> slots;
     std::vector<SeedEntry> seeds;
@@ -125,6 +146,7 @@ struct Pool {
     int lane_ctas = 4;        // CTAs per lane (pa_set_lanes)
     int lane_cap = 0;         // log2 of the cyclic length the lanes are sized for (0: the batch's largest)
     bool batch_lanes = false; // the pending batch ran on the lanes
+    ServeLoop* serve = nullptr;
 };
 
 namespace {
@@ -625,6 +647,67 @@ int lanes_batch(pa_engine* e, Pool* p, const pa_job* jobs, uint32_t count, uint3
     return PA_OK;
 }
 
+// ---------------------------------------------------------------------------------- serving loop
+void free_serve(Pool* p) {
+    ServeLoop* sv = p->serve;
+    if (!sv) return;
+    if (sv->ctl) sv->ctl->stop = 1;
+    if (sv->launched) cudaEventSynchronize(sv->ended);  // the loop ends once it sees stop (bounded)
+    if (sv->s) cudaStreamSynchronize(sv->s);
+    cudaFreeHost(sv->ring);
+    cudaFreeHost(sv->ctl);
+    cudaFree(sv->claimed);
+    cudaFree(sv->lane_job);
+    cudaFree(sv->lane_stats);
+    if (sv->ended) cudaEventDestroy(sv->ended);
+    if (sv->s) cudaStreamDestroy(sv->s);
+    delete sv;
+    p->serve = nullptr;
+}
+
+// (Re)launches the serving loop on the lanes; `claimed` keeps counting across launches.
+int serve_launch(pa_engine* e, Pool* p) {
+    ServeLoop* sv = p->serve;
+    LaneSet* ls = p->lanes;
+    PA_CUDA(e, cudaMemsetAsync(ls->ctl, 0, (1 + 3 * (size_t)ls->lanes) * sizeof(unsigned int), sv->s));
+    pa::LaneArgs a = lane_args(ls, nullptr, 0);
+    a.serve = 1;
+    a.ring = sv->d_ring;
+    a.ring_size = sv->size;
+    a.host = sv->d_ctl;
+    a.claimed = sv->claimed;
+    a.lane_job = sv->lane_job;
+    a.lane_stats = sv->lane_stats;
+    a.idle_ns = sv->idle_ns;
+    int rc = pa::launch_lanes(a, ls->lanes * ls->T, ls->smem, sv->s);
+    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    PA_CUDA(e, cudaEventRecord(sv->ended, sv->s));
+    sv->launched = true;
+    return PA_OK;
+}
+
+bool serve_running(ServeLoop* sv) { return sv->launched && cudaEventQuery(sv->ended) == cudaErrorNotReady; }
+
+// The address the device uses for a served request's buffer: device or managed memory as it is, pinned
+// host memory through its device mapping; anything else (pageable memory) is refused, since the lanes
+// read and write these buffers directly.
+bool device_view(const void* p, const void** out) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+        *out = p;
+        return true;
+    }
+    if (at.type == cudaMemoryTypeHost && at.devicePointer) {
+        *out = at.devicePointer;
+        return true;
+    }
+    return false;
+}
+
 // A slot for an exact recompute of a block of cyclic length 2^cap (one is made if none is idle).
 int exact_slot(pa_engine* e, Pool* p, int cap, Slot** out) {
     for (Slot* c : p->slots)
@@ -647,6 +730,7 @@ int exact_slot(pa_engine* e, Pool* p, int cap, Slot** out) {
 void pool_destroy(pa_engine* e) {
     Pool* p = e->pool;
     if (!p) return;
+    free_serve(p);
     drop_graphs(p);
     free_lanes(p);
     for (Slot* sl : p->slots) free_slot(p, sl);
@@ -688,7 +772,7 @@ int pa_set_lanes(pa_engine* e, int32_t ctas_per_lane, uint32_t max_np) {
     PA_CUDA(e, cudaSetDevice(e->device));
     Pool* p = get_pool(e);
     if (!p) return PA_ERR_CUDA;
-    if (p->batch_pending) return PA_ERR_BUSY;
+    if (p->batch_pending || p->serve) return PA_ERR_BUSY;
     const int cap = max_np ? ceil_log2(max_np) : 0;
     if (cap > pa::kLaneMaxLogNp) return PA_ERR_TOO_LARGE;
     const int T = ctas_per_lane ? ctas_per_lane : 4;
@@ -812,6 +896,7 @@ int pa_batch_run(pa_engine* e, const pa_job* jobs, uint32_t count, uint32_t batc
     Pool* p = get_pool(e);
     if (!p) return PA_ERR_CUDA;
     if (any_busy(p) || p->batch_pending) return PA_ERR_BUSY;
+    if (p->serve && (batch_flags & PA_BATCH_PERSISTENT)) return PA_ERR_BUSY;  // the lanes are serving
     std::vector<BlockGeom> geoms(count);
     int need_cap = 0;
     for (uint32_t i = 0; i < count; ++i) {
@@ -1097,6 +1182,212 @@ int pa_poll(pa_engine* e, uint64_t ticket, pa_stats* stats) {
     }
     sl->busy = false;
     sl->last_use = ++p->clock;
+    return PA_OK;
+}
+
+int pa_serve_start(pa_engine* e, int32_t ctas_per_lane, uint32_t max_np, int32_t ring_slots) {
+    if (!e || ctas_per_lane < 0 || ring_slots < 0 || ring_slots > (1 << 20)) return PA_ERR_INVALID_ARG;
+    if (!max_np || (max_np & (max_np - 1u))) return PA_ERR_INVALID_ARG;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    Pool* p = get_pool(e);
+    if (!p) return PA_ERR_CUDA;
+    if (p->serve || p->batch_pending || any_busy(p)) return PA_ERR_BUSY;
+    const int cap = std::max(ceil_log2(max_np), pa::kLaneMinLogNp);
+    if (cap > pa::kLaneMaxLogNp) return PA_ERR_TOO_LARGE;
+    const int T = ctas_per_lane ? ctas_per_lane : 38;
+    if (p->lanes && (p->lanes->T != T || p->lanes->cap < cap)) free_lanes(p);
+    p->lane_ctas = T;
+    int rc = ensure_lanes(e, p, cap);
+    if (rc) return rc;
+    LaneSet* ls = p->lanes;
+    // lane spectra of every cached static seed, for its own geometry (one launch, synchronous)
+    std::vector<pa::LaneJob> builds;
+    for (size_t i = 0; i < p->seeds.size(); ++i) {
+        const SeedEntry& se = p->seeds[i];
+        if (!se.live) continue;
+        BlockGeom lg;
+        if (lane_geom(se.g.n, se.g.v, se.g.out_bits == se.g.v ? PA_FLAG_COMPRESS : 0u, &lg) || lg.log_np > ls->cap)
+            continue;
+        const auto key = lane_spec_key((int32_t)i, lg);
+        if (ls->spectra.count(key)) continue;
+        LaneSpec sp;
+        sp.bytes = (size_t(1) << lg.log_n) * sizeof(float2) + 32;
+        if (p->used + sp.bytes > p->budget) return PA_ERR_TOO_LARGE;
+        cudaError_t err = cudaMalloc(&sp.spec, (size_t(1) << lg.log_n) * sizeof(float2));
+        if (err == cudaSuccess) err = cudaMalloc(&sp.cnt, 4 * sizeof(unsigned long long));
+        if (err != cudaSuccess) {
+            cudaFree(sp.spec);
+            return cuda_fail(e, err);
+        }
+        p->used += sp.bytes;
+        ls->spectra[key] = sp;
+        pa::LaneJob b{};
+        b.seed = se.seed;
+        b.spec_out = sp.spec;
+        b.cnt = sp.cnt;
+        b.resid = reinterpret_cast<unsigned int*>(sp.cnt + 2);
+        b.g = lg;
+        builds.push_back(b);
+    }
+    if (!builds.empty()) {
+        rc = lanes_launch(e, ls, builds, e->stream);
+        if (rc) return rc;
+        PA_CUDA(e, cudaStreamSynchronize(e->stream));
+    }
+    ServeLoop* sv = new (std::nothrow) ServeLoop();
+    if (!sv) return PA_ERR_INVALID_ARG;
+    p->serve = sv;
+    sv->size = ring_slots ? (uint32_t)ring_slots : 64u;
+    cudaError_t err = cudaHostAlloc((void**)&sv->ring, sv->size * sizeof(pa::ServeSlot), cudaHostAllocMapped);
+    if (err == cudaSuccess) err = cudaHostAlloc((void**)&sv->ctl, sizeof(pa::ServeCtl), cudaHostAllocMapped);
+    if (err == cudaSuccess) err = cudaHostGetDevicePointer((void**)&sv->d_ring, sv->ring, 0);
+    if (err == cudaSuccess) err = cudaHostGetDevicePointer((void**)&sv->d_ctl, sv->ctl, 0);
+    if (err == cudaSuccess) err = cudaMalloc(&sv->claimed, sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaMalloc(&sv->lane_job, (size_t)ls->lanes * sizeof(pa::LaneJob));
+    if (err == cudaSuccess) err = cudaMalloc(&sv->lane_stats, (size_t)ls->lanes * 4 * sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaMemset(sv->claimed, 0, sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&sv->ended, cudaEventDisableTiming);
+    if (err != cudaSuccess) {
+        free_serve(p);
+        return cuda_fail(e, err);
+    }
+    std::memset(sv->ring, 0, sv->size * sizeof(pa::ServeSlot));
+    std::memset(sv->ctl, 0, sizeof(pa::ServeCtl));
+    sv->owner.assign(sv->size, ~0ull);
+    sv->jobs.assign(sv->size, pa_job{});
+    sv->geoms.assign(sv->size, BlockGeom{});
+    rc = serve_launch(e, p);
+    if (rc) {
+        free_serve(p);
+        return rc;
+    }
+    return ls->lanes;
+}
+
+int pa_serve_submit(pa_engine* e, const pa_job* job, uint64_t* ticket) {
+    if (!e || !job || !ticket) return PA_ERR_INVALID_ARG;
+    Pool* p = e->pool;
+    if (!p || !p->serve) return PA_ERR_INVALID_ARG;
+    ServeLoop* sv = p->serve;
+    LaneSet* ls = p->lanes;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    BlockGeom g, lg;
+    int rc = job_geom(e, p, *job, &g);
+    if (rc) return rc;
+    rc = lane_geom(job->n, job->v, job->flags, &lg);
+    if (rc) return rc;
+    if (lg.log_np > ls->cap) return PA_ERR_TOO_LARGE;
+    if (reinterpret_cast<uintptr_t>(job->out) & 3u) return PA_ERR_INVALID_ARG;
+    const uint32_t k = (uint32_t)(sv->next_ticket % sv->size);
+    if (sv->owner[k] != ~0ull) return PA_ERR_BUSY;  // the ring is full: collect with pa_serve_poll
+    pa::LaneJob j{};
+    const void *ks = nullptr, *kr = nullptr, *sd = nullptr, *out = nullptr;
+    if (!device_view(job->key_start, &ks) || !device_view(job->out, &out)) return PA_ERR_INVALID_ARG;
+    if ((job->flags & PA_FLAG_XOR_KEY_REST) && !device_view(job->key_rest, &kr)) return PA_ERR_INVALID_ARG;
+    j.key_start = static_cast<const uint32_t*>(ks);
+    j.key_rest = static_cast<const uint32_t*>(kr);
+    if (job->seed_id >= 0) {
+        auto it = ls->spectra.find(lane_spec_key(job->seed_id, lg));
+        if (it == ls->spectra.end()) return PA_ERR_NO_SEED;  // cache the seed before pa_serve_start
+        j.spec = it->second.spec;
+        j.seed_cnt = it->second.cnt + 1;
+    } else {
+        if (!device_view(job->seed_words, &sd)) return PA_ERR_INVALID_ARG;
+        j.seed = static_cast<const uint32_t*>(sd);
+    }
+    j.out = static_cast<uint32_t*>(const_cast<void*>(out));
+    j.g = lg;
+    j.flags = job->flags;
+    pa::ServeSlot* slot = sv->ring + k;
+    slot->job = j;
+    slot->err = 0;
+    __atomic_store_n(&slot->done, 0ull, __ATOMIC_RELAXED);
+    sv->owner[k] = sv->next_ticket;
+    sv->jobs[k] = *job;
+    sv->geoms[k] = g;
+    *ticket = sv->next_ticket++;
+    __atomic_store_n(&sv->ctl->tail, sv->next_ticket, __ATOMIC_RELEASE);  // publish
+    if (!serve_running(sv)) {  // the loop ended (idle): start it again
+        rc = serve_launch(e, p);
+        if (rc) return rc;
+    }
+    return PA_OK;
+}
+
+int pa_serve_poll(pa_engine* e, uint64_t ticket, pa_stats* stats) {
+    if (!e) return PA_ERR_INVALID_ARG;
+    Pool* p = e->pool;
+    if (!p || !p->serve) return PA_ERR_INVALID_ARG;
+    ServeLoop* sv = p->serve;
+    const uint32_t k = (uint32_t)(ticket % sv->size);
+    if (sv->owner[k] != ticket) return PA_ERR_INVALID_ARG;
+    pa::ServeSlot* slot = sv->ring + k;
+    if (__atomic_load_n(&slot->done, __ATOMIC_ACQUIRE) != ticket + 1ull) {
+        if (serve_running(sv)) return PA_PENDING;
+        PA_CUDA(e, cudaSetDevice(e->device));
+        cudaError_t q = cudaEventQuery(sv->ended);
+        if (q != cudaSuccess && q != cudaErrorNotReady) return cuda_fail(e, q);
+        std::vector<int> lerr(p->lanes->lanes);
+        PA_CUDA(e, cudaMemcpy(lerr.data(), p->lanes->ctl + 1 + 2 * p->lanes->lanes, lerr.size() * sizeof(int),
+                              cudaMemcpyDeviceToHost));
+        for (int x : lerr)
+            if (x) {  // a bounded wait of the loop expired: this request will not complete
+                sv->owner[k] = ~0ull;
+                e->last_cuda = (int)cudaErrorLaunchTimeout;
+                return PA_ERR_CUDA;
+            }
+        if (__atomic_load_n(&slot->done, __ATOMIC_ACQUIRE) == ticket + 1ull) return PA_PENDING;  // just finished
+        int rc = serve_launch(e, p);  // the loop ended idle before this request was published
+        return rc ? rc : PA_PENDING;
+    }
+    if (slot->err) {
+        sv->owner[k] = ~0ull;
+        e->last_cuda = (int)cudaErrorLaunchTimeout;
+        return PA_ERR_CUDA;
+    }
+    float r;
+    std::memcpy(&r, &slot->resid, sizeof(r));
+    int exact = 0;
+    if (!(r <= e->residual_limit)) {  // FP32 budget exceeded: recompute exactly from the host inputs
+        PA_CUDA(e, cudaSetDevice(e->device));
+        const pa_job& jb = sv->jobs[k];
+        const BlockGeom& g = sv->geoms[k];
+        Slot* sl = nullptr;
+        int rc = exact_slot(e, p, g.log_np, &sl);
+        if (rc) return rc;
+        const uint32_t* seed = jb.seed_id >= 0 ? p->seeds[jb.seed_id].seed : sl->seed;
+        if (jb.seed_id < 0)
+            PA_CUDA(e, cudaMemcpyAsync(sl->seed, jb.seed_words, (size_t)(jb.n / 32u) * 4u, cudaMemcpyHostToDevice,
+                                       sl->s));
+        PA_CUDA(e, cudaMemcpyAsync(sl->ks, jb.key_start, (size_t)(g.h / 32u + 1u) * 4u, cudaMemcpyHostToDevice, sl->s));
+        if (jb.flags & PA_FLAG_XOR_KEY_REST)
+            PA_CUDA(e, cudaMemcpyAsync(sl->kr, jb.key_rest, (size_t)(jb.v / 32u) * 4u, cudaMemcpyHostToDevice, sl->s));
+        rc = exact_in_slot(e, sl, g, seed, sl->ks, sl->kr, jb.flags, sl->out, sl->s);
+        if (rc) return rc;
+        PA_CUDA(e, cudaMemcpyAsync(jb.out, sl->out, pa_output_bytes(jb.n, jb.v, jb.flags), cudaMemcpyDeviceToHost,
+                                   sl->s));
+        PA_CUDA(e, cudaStreamSynchronize(sl->s));
+        exact = 1;
+    }
+    if (stats) {
+        stats->max_residual = r;
+        stats->popcount_key = slot->cnt[0];
+        stats->popcount_seed = slot->cnt[1];
+        stats->gpu_ms = 0.f;
+        stats->seed_uses_left = -1;
+        stats->exact = exact;
+    }
+    sv->owner[k] = ~0ull;
+    return PA_OK;
+}
+
+int pa_serve_stop(pa_engine* e) {
+    if (!e) return PA_ERR_INVALID_ARG;
+    Pool* p = e->pool;
+    if (!p || !p->serve) return PA_OK;
+    PA_CUDA(e, cudaSetDevice(e->device));
+    free_serve(p);
     return PA_OK;
 }
 

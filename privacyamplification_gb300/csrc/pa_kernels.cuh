@@ -23,14 +23,17 @@ struct BlockGeom {
 //   s'[x] = s[x]               for x < seed_direct = min(Np - h, n),
 //   s'[x] = s[x - (Np - n)]    for x >= Np - h.
 // Positions in between (present when n + h < Np) are read by no output i < out_bits; they are filled
-// with seed bits s[x - seed_direct] (an index below n) rather than zeros: a long run of zeros would
-// give the placed seed large near-DC spectral coefficients and cost the FP32 path most of its
-// rounding budget.
+// with seed bits s[(x - seed_direct) mod n] rather than zeros: a long run of zeros would give the placed
+// seed large near-DC spectral coefficients and cost the FP32 path most of its rounding budget.  With the
+// smallest Np (below 2n) the index x - seed_direct is already below n; a larger Np (the persistent lanes
+// place every block in at least 2^20) needs the reduction, or the filler would read past the seed.
 __host__ __device__ inline int seed_source(const BlockGeom& g, uint64_t x, uint64_t* src) {
     uint64_t np = 1ull << g.log_np;
     if (x < g.seed_direct) { *src = x; return 1; }
     if (x >= np - g.h) { *src = x - (np - g.n); return 1; }
-    *src = x - g.seed_direct;
+    uint64_t f = x - g.seed_direct;
+    if (f >= g.n) f %= g.n;
+    *src = f;
     return 1;
 }
 

@@ -21,6 +21,19 @@ __device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
     return v;
 }
 __device__ __forceinline__ int ld_volatile(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+__device__ __forceinline__ unsigned long long ld_acquire_sys_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void st_release_sys_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
 // Inputs: device memory written before the launch (L2 loads), or host memory the host may have
@@ -37,7 +50,8 @@ __device__ __forceinline__ bool lane_sync(const LaneArgs& a, int lane, unsigned 
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        __threadfence();
+        if (a.serve) __threadfence_system();  // served outputs go to host memory: visible to the host too
+        else __threadfence();
         atomicAdd(a.bar + lane, 1u);
         for (uint32_t i = 0; (int)(ld_acquire_gpu(a.bar + lane) - target) < 0; ++i) {
             if (ld_volatile(a.err + lane)) {
@@ -309,35 +323,109 @@ __device__ __forceinline__ bool lane_block(const LaneArgs& a, const LaneJob& j, 
 
 }  // namespace
 
-// The lane loop: rank 0 of a lane takes the next block (atomic counter over the job list, longest first)
-// and clears its counters; a lane barrier hands the block to the lane's other CTAs, which also separates
-// the previous block's last stage from this block's first.
+// Batch: the next block of the list (atomic counter, longest first), its counters cleared.
+__device__ __forceinline__ int batch_claim(const LaneArgs& a, int lane) {
+    if (ld_volatile(a.err + lane)) return kLaneExit;
+    const unsigned int k = atomicAdd(a.next, 1u);
+    if (k >= a.njobs) return kLaneExit;
+    const LaneJob& jb = a.jobs[k];
+    jb.cnt[0] = 0ull;
+    jb.cnt[1] = jb.seed_cnt ? *jb.seed_cnt : 0ull;
+    *jb.resid = 0u;
+    return (int)k;
+}
+
+// Serving loop: the next published request (ticket) not yet taken by any lane; its descriptor is copied
+// from the host ring into the lane's device slot with the lane's counters.  With nothing published the
+// lane idles (a short sleep), and it ends when the host asks it to or after idle_ns without a request.
+__device__ __forceinline__ int serve_claim(const LaneArgs& a, int lane, unsigned long long& idle_since) {
+    if (ld_volatile(a.err + lane)) return kLaneExit;
+    const unsigned long long tail = ld_acquire_sys_u64(&a.host->tail);
+    for (;;) {
+        const unsigned long long c = *reinterpret_cast<volatile unsigned long long*>(a.claimed);
+        if (c >= tail) break;
+        if (atomicCAS(a.claimed, c, c + 1ull) != c) continue;
+        const volatile LaneJob* src = &a.ring[c % a.ring_size].job;
+        LaneJob j;
+        j.key_start = src->key_start;
+        j.key_rest = src->key_rest;
+        j.seed = src->seed;
+        j.spec = src->spec;
+        j.spec_out = nullptr;
+        j.out = src->out;
+        j.seed_cnt = src->seed_cnt;
+        j.g.n = src->g.n;
+        j.g.v = src->g.v;
+        j.g.h = src->g.h;
+        j.g.out_bits = src->g.out_bits;
+        j.g.log_np = src->g.log_np;
+        j.g.log_n = src->g.log_n;
+        j.g.log_n1 = src->g.log_n1;
+        j.g.log_n2 = src->g.log_n2;
+        j.g.seed_direct = src->g.seed_direct;
+        j.g.exact_only = src->g.exact_only;
+        j.flags = src->flags;
+        unsigned long long* st = a.lane_stats + 4 * lane;
+        j.cnt = st;
+        j.resid = reinterpret_cast<unsigned int*>(st + 2);
+        j.pad_ = 0;
+        st[0] = 0ull;
+        st[1] = j.seed_cnt ? *j.seed_cnt : 0ull;
+        st[2] = 0ull;
+        st[3] = c;  // the ticket, for the completion
+        a.lane_job[lane] = j;
+        idle_since = 0;
+        return 0;
+    }
+    if (*reinterpret_cast<volatile int*>(&a.host->stop)) return kLaneExit;
+    const unsigned long long now = global_ns();
+    if (!idle_since) idle_since = now;
+    else if (now - idle_since > a.idle_ns) return kLaneExit;
+    __nanosleep(2000);
+    return kLaneIdle;
+}
+
+// Completion of the lane's last request, once every CTA of the lane has passed the barrier after its
+// finish stage: statistics into the host slot, then done = ticket + 1 (release at system scope).
+__device__ __forceinline__ void serve_publish(const LaneArgs& a, int lane) {
+    const unsigned long long* st = a.lane_stats + 4 * lane;
+    const unsigned long long tk = st[3];
+    ServeSlot* s = a.ring + (tk % a.ring_size);
+    volatile ServeSlot* vs = s;
+    vs->cnt[0] = st[0];
+    vs->cnt[1] = st[1];
+    vs->resid = *reinterpret_cast<const unsigned int*>(st + 2);
+    vs->err = ld_volatile(a.err + lane);
+    __threadfence_system();
+    st_release_sys_u64(&s->done, tk + 1ull);
+}
+
+// The lane loop: rank 0 of a lane takes the next block and writes its index to the lane's slot; a lane
+// barrier hands it to the lane's other CTAs, which also separates the previous block's last stage from
+// this block's first.
 __global__ void __launch_bounds__(kLaneThreads, 1) k_lanes(const __grid_constant__ LaneArgs a) {
     const int lane = (int)blockIdx.x / a.T, rank = (int)blockIdx.x % a.T;
     if (lane >= a.lanes) return;
     __shared__ int s_job;
     unsigned int target = 0;
+    unsigned long long idle_since = 0;
+    bool served = false;  // a request of this lane waits for its completion to be published
     for (;;) {
         if (rank == 0 && threadIdx.x == 0) {
-            int j = -1;
-            if (!ld_volatile(a.err + lane)) {
-                const unsigned int k = atomicAdd(a.next, 1u);
-                if (k < a.njobs) {
-                    j = (int)k;
-                    const LaneJob& jb = a.jobs[k];
-                    jb.cnt[0] = 0ull;
-                    jb.cnt[1] = jb.seed_cnt ? *jb.seed_cnt : 0ull;
-                    *jb.resid = 0u;
-                }
-            }
+            const int j = a.serve ? serve_claim(a, lane, idle_since) : batch_claim(a, lane);
             *reinterpret_cast<volatile int*>(a.slot + lane) = j;
         }
-        if (!lane_sync(a, lane, target)) break;
+        const bool ok = lane_sync(a, lane, target);
+        if (served && rank == 0 && threadIdx.x == 0) serve_publish(a, lane);
+        served = false;
+        if (!ok) break;
         if (threadIdx.x == 0) s_job = ld_volatile(a.slot + lane);
         __syncthreads();
         const int j = s_job;
+        if (j == kLaneIdle) continue;
         if (j < 0) break;
-        if (!lane_block(a, a.jobs[j], false, lane, rank, target)) break;
+        if (!lane_block(a, a.serve ? a.lane_job[lane] : a.jobs[j], a.serve != 0, lane, rank, target)) break;
+        served = a.serve != 0;
     }
 }
 

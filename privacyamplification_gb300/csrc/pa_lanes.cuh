@@ -48,6 +48,24 @@ struct LaneJob {
     uint32_t pad_;
 };
 
+// One request of the serving loop, in pinned host memory: the host fills `job` (its pointers are host
+// pointers the device can reach, or device pointers) and publishes the request by raising the ring's
+// tail; the lane that served it writes the statistics and then done = ticket + 1.
+struct ServeSlot {
+    LaneJob job;
+    unsigned long long cnt[2];
+    unsigned int resid;
+    int err;
+    unsigned long long done;
+};
+
+// Host-memory words of the serving loop.
+struct ServeCtl {
+    unsigned long long tail;  // requests published (tickets 0 .. tail-1)
+    int stop;                 // the host asks the loop to end once every published request is taken
+    int pad_;
+};
+
 struct LaneArgs {
     const LaneJob* jobs;
     uint32_t njobs;
@@ -66,12 +84,22 @@ struct LaneArgs {
     int early_b[kLaneMaps];  // pass B boxes copied ahead, per log_n1
     int early_c[kLaneMaps];  // pass C boxes copied ahead, per log_n1
     uint32_t wait_limit;     // lane-barrier poll rounds before giving up
+    // serving loop (serve != 0): requests come from a ring of host slots instead of `jobs`
+    int serve;
+    ServeSlot* ring;                 // host memory, ring_size slots; ticket t uses slot t % ring_size
+    uint32_t ring_size;
+    ServeCtl* host;                  // host memory
+    unsigned long long* claimed;     // device: tickets taken so far
+    LaneJob* lane_job;               // device, per lane: the request being served
+    unsigned long long* lane_stats;  // device, per lane: cnt[2], resid word
+    unsigned long long idle_ns;      // time without a request after which the loop ends by itself
 };
 
 // Host side (pa_lanes.cu).
 size_t lane_smem_bytes();                                    // dynamic shared memory of the lane kernel
 int lane_early_boxes(int log_n1, int pass, size_t dyn_bytes);  // pass 'b' or 'c'
 int launch_lanes(const LaneArgs& a, int grid, size_t smem, cudaStream_t s);
+constexpr int kLaneIdle = -2, kLaneExit = -1;  // slot values besides a job index
 int make_lane_maps(const float2* Y, const float2* Z, CUtensorMap* out /* kLaneMaps * 2 */);
 int lane_max_ctas(int* ctas);  // resident CTAs of the lane kernel on the current device
 

@@ -9,6 +9,9 @@ hash bits.  Key material is drawn from fixed-seed PCG64 streams as i.i.d. Bernou
 * poisson_requests() + serve(): requests arrive at exponential inter-arrival times; serve() admits
   each to a free slot as soon as one is free (continuous batching: blocks of different sizes overlap on
   the GPU), polls for completions and records latency = completion - arrival.
+* serve_device(): the same arrivals through the device-resident serving loop (pa_serve_*): the host
+  only publishes request descriptors and reads completions; lanes on the GPU take requests as they free
+  up, read the inputs from pinned host memory and write the outputs there.
 """
 from __future__ import annotations
 
@@ -231,6 +234,63 @@ def serve(engine, reqs, banks, out_slots=24, keep=lambda r: False, seed_ids=None
             progressed = True
         for t in list(inflight):
             st = engine.poll(t)
+            if st is None:
+                continue
+            r, ob = inflight.pop(t)
+            r.done = time.perf_counter() - t0
+            r.exact = st.exact
+            res.exact += st.exact
+            res.latency_ms.append((r.done - r.arrival) * 1e3)
+            res.bits += r.n
+            if keep(r):
+                res.outputs[r.rid] = outs[ob][: output_bytes(r.n, r.v, r.flags)].copy()
+            free_out.append(ob)
+            remaining -= 1
+            progressed = True
+        if not progressed:
+            if not inflight and not waiting and pending:
+                time.sleep(max(0.0, min(pending[0].arrival - (time.perf_counter() - t0), 1e-3)))
+            else:
+                time.sleep(idle_sleep)
+    res.wall_s = time.perf_counter() - t0
+    return res
+
+
+def serve_device(engine, reqs, banks, out_slots=24, keep=lambda r: False, seed_ids=None, idle_sleep=20e-6):
+    """Serves `reqs` in real time through the device-resident loop (engine.serve_start() first); returns
+    latencies and the outputs of requests `keep` selects.  Admission is FIFO: a request waits for a free
+    pinned output buffer and a free ring slot; the device takes published requests as lanes free up."""
+    import torch
+    max_out = max(output_bytes(r.n, r.v, r.flags) for r in reqs)
+    outs = [torch.empty(max_out + 4, dtype=torch.uint8).pin_memory().numpy() for _ in range(out_slots)]
+    free_out = list(range(out_slots))
+    pending = deque(sorted(reqs, key=lambda r: r.arrival))
+    waiting = deque()
+    inflight = {}
+    res = ServeResult(latency_ms=[], wall_s=0.0, bits=0)
+    t0 = time.perf_counter()
+    remaining = len(reqs)
+    while remaining:
+        now = time.perf_counter() - t0
+        progressed = False
+        while pending and pending[0].arrival <= now:
+            waiting.append(pending.popleft())
+        while waiting and free_out:
+            r = waiting[0]
+            ob = free_out[-1]
+            sid = seed_ids[seed_key(r.n, r.v, r.flags)] if (r.static and seed_ids is not None) else -1
+            seed = None if sid >= 0 else banks.seed_words(r)
+            job = PAJob(seed.ctypes.data if seed is not None else None, sid, banks.key_start(r).ctypes.data,
+                        banks.key_rest(r).ctypes.data, r.n, r.v, r.flags, outs[ob].ctypes.data)
+            t = engine.serve_submit(job)
+            if t is None:
+                break
+            free_out.pop()
+            waiting.popleft()
+            inflight[t] = (r, ob)
+            progressed = True
+        for t in list(inflight):
+            st = engine.serve_poll(t)
             if st is None:
                 continue
             r, ob = inflight.pop(t)
