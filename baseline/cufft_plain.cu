@@ -32,6 +32,18 @@
 
 namespace {
 
+// The reference's own kernels (binInt2float, calculateCorrectionFloat, setFirstElementToZero,
+// ElementWiseProduct, ToBinaryArray[NoXOR]), compiled for sm_103a from PrivacyAmplification.cu by
+// baseline/ref_cuda.py into a fatbin and loaded at run time (cp_load_reference).  When they are loaded,
+// cp_process launches them, with the reference's launch shapes and its __constant__ values, in place of
+// the restated kernels below; cuFFT, the pinned slots and the host syncs are the same either way.
+struct RefKernels {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t unpack = nullptr, corr = nullptr, zero = nullptr, product = nullptr, pack = nullptr,
+                 pack_noxor = nullptr;
+};
+RefKernels g_ref;
+
 constexpr float kH1 = 1.0f / 2048.0f;  // 1 / 2^reduction_exp
 constexpr float kR = 32.0f;            // 2^pre_mul_reduction_exp
 
@@ -211,19 +223,41 @@ CP_API int cp_process(void* h, int recalc_seed, int do_xor, int do_compress, dou
     };
     for (double& x : p->step_ms) x = 0.0;
     cudaStream_t s = p->s;
+    const bool ref = g_ref.lib != nullptr;
+    auto launch = [&](cudaKernel_t k, uint32_t grid, uint32_t block, void** args) {
+        return cudaLaunchKernel(reinterpret_cast<const void*>(k), dim3(grid), dim3(block), args, 0, s);
+    };
+    uint32_t* cnt_seed = p->cnt;
+    uint32_t* cnt_key = p->cnt + 1;
     if (seed) {
         CP_TRY(cudaMemsetAsync(p->cnt, 0, 2 * sizeof(uint32_t), s));
-        k_unpack<<<(n + 1023u) / 1024u, 1024, 0, s>>>(p->h_seed, p->di2, p->cnt);
+        if (ref) {
+            void* a[] = {&p->h_seed, &p->di2, &cnt_seed};
+            CP_TRY(launch(g_ref.unpack, (n + 1023u) / 1024u, n < 1024u ? n : 1024u, a));
+        } else {
+            k_unpack<<<(n + 1023u) / 1024u, 1024, 0, s>>>(p->h_seed, p->di2, p->cnt);
+        }
         CP_TRY(cudaStreamSynchronize(s));
     } else {
         CP_TRY(cudaMemsetAsync(p->cnt + 1, 0, sizeof(uint32_t), s));
     }
     mark(0);
     const uint32_t key_words = hl / 32u + 1u;
-    k_unpack<<<(key_words * 32u + 1023u) / 1024u, 1024, 0, s>>>(p->h_ks, p->di1, p->cnt + 1);
+    if (ref) {
+        void* a[] = {&p->h_ks, &p->di1, &cnt_key};
+        CP_TRY(launch(g_ref.unpack, (key_words * 32u + 1023u) / 1024u, key_words * 32u < 1024u ? key_words * 32u : 1024u,
+                      a));
+    } else {
+        k_unpack<<<(key_words * 32u + 1023u) / 1024u, 1024, 0, s>>>(p->h_ks, p->di1, p->cnt + 1);
+    }
     CP_TRY(cudaStreamSynchronize(s));
     mark(1);
-    k_correction<<<1, 1, 0, s>>>(p->cnt, p->corr, n);
+    if (ref) {
+        void* a[] = {&cnt_seed, &cnt_key, &p->corr};
+        CP_TRY(launch(g_ref.corr, 1, 1, a));
+    } else {
+        k_correction<<<1, 1, 0, s>>>(p->cnt, p->corr, n);
+    }
     CP_TRY(cudaStreamSynchronize(s));
     mark(2);
     CP_FFT(cufftSetStream(p->fwd, s));
@@ -236,10 +270,17 @@ CP_API int cp_process(void* h, int recalc_seed, int do_xor, int do_compress, dou
         p->seed_ready = true;
     }
     mark(4);
-    k_zero_dc<<<1, 2, 0, s>>>(p->do1, p->do2);
-    CP_TRY(cudaStreamSynchronize(s));
     const uint32_t bins = n / 2u + 1u;
-    k_product<<<(bins + 1023u) / 1024u, bins < 1024u ? bins : 1024u, 0, s>>>(p->do1, p->do2, bins);
+    if (ref) {
+        void* a[] = {&p->do1, &p->do2};
+        CP_TRY(launch(g_ref.zero, 1, 2, a));
+        CP_TRY(cudaStreamSynchronize(s));
+        CP_TRY(launch(g_ref.product, (bins + 1023u) / 1024u, bins < 1024u ? bins : 1024u, a));
+    } else {
+        k_zero_dc<<<1, 2, 0, s>>>(p->do1, p->do2);
+        CP_TRY(cudaStreamSynchronize(s));
+        k_product<<<(bins + 1023u) / 1024u, bins < 1024u ? bins : 1024u, 0, s>>>(p->do1, p->do2, bins);
+    }
     CP_TRY(cudaStreamSynchronize(s));
     mark(5);
     CP_FFT(cufftSetStream(p->inv, s));
@@ -248,7 +289,16 @@ CP_API int cp_process(void* h, int recalc_seed, int do_xor, int do_compress, dou
     mark(6);
     const float norm = (float)n / (2048.0f * kR) / (2048.0f * kR);
     uint32_t* out = reinterpret_cast<uint32_t*>(p->h_out);
-    if (do_xor) {
+    if (ref) {
+        if (do_xor) {
+            void* a[] = {&p->di2, &out, &p->h_kr, &p->corr};
+            CP_TRY(launch(g_ref.pack, p->v / 32u / 31u + 1u, 1023, a));
+        } else {
+            const uint32_t words = do_compress ? p->v / 32u : n / 64u;
+            void* a[] = {&p->di2, &out, &p->corr};
+            CP_TRY(launch(g_ref.pack_noxor, words / 31u + 1u, 1023, a));
+        }
+    } else if (do_xor) {
         k_pack<true><<<p->v / 32u / 31u + 1u, 1023, 0, s>>>(p->di2, out, p->h_kr, p->corr, norm);
     } else {
         const uint32_t words = do_compress ? p->v / 32u : n / 64u;
@@ -277,4 +327,74 @@ CP_API int cp_residual(void* h, uint32_t out_bits, float* max_resid) {
     CP_TRY(cudaMemcpyAsync(max_resid, p->resid, sizeof(float), cudaMemcpyDeviceToHost, p->s));
     CP_TRY(cudaStreamSynchronize(p->s));
     return 0;
+}
+
+// Loads the reference's kernels from a fatbin built from PrivacyAmplification.cu (baseline/ref_cuda.py)
+// and sets their __constant__ values for blocks of n bits (PrivacyAmplification.cu:1597-1606, 1729-1732):
+// c0 = 0, h0 = 0, h1_reduced = 2^-11, sample_size = n, pre_mul_reduction = 2^5,
+// normalisation_float = n / (2^11 2^5)^2.  Returns 0, or a negative code when the file or a kernel is
+// missing.  From then on cp_process launches the reference's kernels (cp_unload_reference undoes it).
+CP_API int cp_load_reference(const char* path, uint32_t n) {
+    cudaLibrary_t lib = g_ref.lib;
+    RefKernels r = g_ref;
+    if (lib) goto constants;  // loaded: only the constants for n
+    if (cudaLibraryLoadFromFile(&lib, path, nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return -4;
+    }
+    {
+    cudaKernel_t ks[64];
+    unsigned int count = 0;
+    if (cudaLibraryGetKernelCount(&count, lib) != cudaSuccess || count == 0 || count > 64 ||
+        cudaLibraryEnumerateKernels(ks, count, lib) != cudaSuccess) {
+        cudaLibraryUnload(lib);
+        return -5;
+    }
+    r.lib = lib;
+    for (unsigned int i = 0; i < count; ++i) {
+        const char* name = nullptr;
+        if (cudaFuncGetName(&name, reinterpret_cast<const void*>(ks[i])) != cudaSuccess || !name) continue;
+        if (std::strstr(name, "binInt2float")) r.unpack = ks[i];
+        else if (std::strstr(name, "calculateCorrectionFloat")) r.corr = ks[i];
+        else if (std::strstr(name, "setFirstElementToZero")) r.zero = ks[i];
+        else if (std::strstr(name, "ElementWiseProduct")) r.product = ks[i];
+        else if (std::strstr(name, "ToBinaryArrayNoXOR")) r.pack_noxor = ks[i];
+        else if (std::strstr(name, "ToBinaryArray")) r.pack = ks[i];
+    }
+    if (!r.unpack || !r.corr || !r.zero || !r.product || !r.pack || !r.pack_noxor) {
+        cudaLibraryUnload(lib);
+        return -6;
+    }
+    }
+constants:
+    const float zero = 0.0f, h1 = kH1, normf = (float)n / (2048.0f * kR) / (2048.0f * kR);
+    const float2 c0 = make_float2(0.f, 0.f);
+    const uint32_t pre = (uint32_t)kR;
+    struct Sym {
+        const char* name;
+        const void* val;
+        size_t bytes;
+    } syms[] = {{"c0_dev", &c0, sizeof(c0)},
+                {"h0_dev", &zero, sizeof(zero)},
+                {"h1_reduced_dev", &h1, sizeof(h1)},
+                {"normalisation_float_dev", &normf, sizeof(normf)},
+                {"sample_size_dev", &n, sizeof(n)},
+                {"pre_mul_reduction_dev", &pre, sizeof(pre)}};
+    for (const Sym& sy : syms) {
+        void* dptr = nullptr;
+        size_t bytes = 0;
+        if (cudaLibraryGetGlobal(&dptr, &bytes, lib, sy.name) != cudaSuccess || bytes != sy.bytes ||
+            cudaMemcpy(dptr, sy.val, sy.bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            if (!g_ref.lib) cudaLibraryUnload(lib);
+            return -7;
+        }
+    }
+    g_ref = r;
+    return 0;
+}
+
+CP_API void cp_unload_reference() {
+    if (g_ref.lib) cudaLibraryUnload(g_ref.lib);
+    g_ref = RefKernels{};
 }

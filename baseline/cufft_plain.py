@@ -50,6 +50,10 @@ class CufftPlain:
         lib.cp_residual.restype = ctypes.c_int
         lib.cp_step_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
         lib.cp_step_ms.restype = None
+        lib.cp_load_reference.argtypes = [ctypes.c_char_p, ctypes.c_uint32]
+        lib.cp_load_reference.restype = ctypes.c_int
+        lib.cp_unload_reference.argtypes = []
+        lib.cp_unload_reference.restype = None
         self._lib, self.n, self.v = lib, n, v
         h = vp()
         rc = lib.cp_create(n, v, ctypes.byref(h))
@@ -78,6 +82,16 @@ class CufftPlain:
             kr = np.asarray(key_rest, np.uint32)
             self.key_rest[:] = 0
             self.key_rest[: kr.size] = kr
+
+    def use_reference_kernels(self, fatbin: str):
+        """From now on (for every pipeline in this process) launch the reference's own kernels, compiled
+        from PrivacyAmplification.cu (baseline/ref_cuda.py), with their constants for this n."""
+        rc = self._lib.cp_load_reference(fatbin.encode(), self.n)
+        if rc != 0:
+            raise RuntimeError("cp_load_reference(%s) failed: %d" % (fatbin, rc))
+
+    def use_restated_kernels(self):
+        self._lib.cp_unload_reference()
 
     def process(self, recalc_seed: bool, do_xor: bool = True, do_compress: bool = True) -> float:
         """Runs one block; returns its host wall time in ms."""

@@ -419,7 +419,7 @@ int lane_geom(uint32_t n, uint32_t v, uint32_t flags, BlockGeom* g) {
     g->log_np = std::max(ceil_log2(need), pa::kLaneMinLogNp);
     if (g->log_np > pa::kLaneMaxLogNp) return PA_ERR_TOO_LARGE;
     const uint64_t np = 1ull << g->log_np;
-    g->seed_direct = np == n ? n : (uint32_t)std::min<uint64_t>(np - g->h, n);
+    g->seed_direct = is_pow2(n) ? n : (uint32_t)std::min<uint64_t>(np - g->h, n);  // pow2: periodic placement
     g->log_n = g->log_np - 1;
     g->log_n2 = pa::kLaneLogRow;
     g->log_n1 = g->log_n - pa::kLaneLogRow;
@@ -494,10 +494,10 @@ int ensure_lanes(pa_engine* e, Pool* p, int cap) {
     return PA_OK;
 }
 
-// Key of a static seed's lane spectrum: the seed and its placement (any v shares the spectrum of a
-// power-of-two n that fills the cyclic length).
+// Key of a static seed's lane spectrum: the seed and its placement (a power-of-two n is placed
+// periodically, so every v shares its spectrum).
 std::array<uint64_t, 4> lane_spec_key(int32_t seed_id, const BlockGeom& g) {
-    const bool identity = (1ull << g.log_np) == g.n;
+    const bool identity = is_pow2(g.n);
     return {(uint64_t)seed_id, (uint64_t)g.log_np, identity ? 0ull : g.seed_direct, identity ? 0ull : g.h};
 }
 

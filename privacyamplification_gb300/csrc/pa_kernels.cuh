@@ -27,8 +27,12 @@ struct BlockGeom {
 // seed large near-DC spectral coefficients and cost the FP32 path most of its rounding budget.  With the
 // smallest Np (below 2n) the index x - seed_direct is already below n; a larger Np (the persistent lanes
 // place every block in at least 2^20) needs the reduction, or the filler would read past the seed.
+// A power-of-two n in a larger Np (the persistent lanes' smallest cyclic length) is placed periodically,
+// s'[x] = s[x mod n]: Np is then a multiple of n, so every output sees s[(i-j) mod n] for any h, and one
+// spectrum serves every v.
 __host__ __device__ inline int seed_source(const BlockGeom& g, uint64_t x, uint64_t* src) {
     uint64_t np = 1ull << g.log_np;
+    if ((g.n & (g.n - 1u)) == 0) { *src = x & (g.n - 1u); return 1; }
     if (x < g.seed_direct) { *src = x; return 1; }
     if (x >= np - g.h) { *src = x - (np - g.n); return 1; }
     uint64_t f = x - g.seed_direct;

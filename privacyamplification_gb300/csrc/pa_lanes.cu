@@ -76,14 +76,18 @@ __device__ __forceinline__ bool lane_sync(const LaneArgs& a, int lane, unsigned 
 
 // ---------------------------------------------------------------------------------------- bit rows
 // Key or seed bits -> bit rows (the transposes of k_bit_rows / k_bit_rows_tiled).  Tiled form (N1 >=
-// 256, seed only when it needs no placement): the two 256-thread halves of the CTA take one 256 x 256
-// tile of 2-bit elements each, per round; otherwise every warp takes 16 rows x 32 columns, one word
-// per lane.  The CTA takes rounds first, first + stride, ...
+// 256, seed only when it is placed word by word): the two 256-thread halves of the CTA take one 256 x 256
+// tile of 2-bit elements each, per round; otherwise every warp takes 16 rows x 32 columns, one word per
+// lane.  The CTA takes rounds first, first + stride, ...
 __device__ __noinline__ void lane_bit_rows(const uint32_t* __restrict__ src, bool seed, bool hostin,
                                               const BlockGeom& g, uint32_t* __restrict__ rows, uint32_t first,
                                               uint32_t stride) {
     const uint32_t n1 = 1u << g.log_n1, n2 = 1u << g.log_n2;
-    const bool placed = seed && (1u << g.log_np) != g.n;
+    // a power-of-two seed repeats with period n (word index mod n/32); any other n in a larger Np is placed
+    // bit by bit (seed_source)
+    const bool periodic = seed && (g.n & (g.n - 1u)) == 0;
+    const bool placed = seed && !periodic && (1u << g.log_np) != g.n;
+    const uint64_t wmask = periodic ? (uint64_t)(g.n / 32u) - 1u : ~0ull;
     const int lane = threadIdx.x & 31;
     if (n1 >= 256u && !placed) {
         extern __shared__ __align__(16) uint32_t lane_smem[];
@@ -101,7 +105,7 @@ __device__ __noinline__ void lane_bit_rows(const uint32_t* __restrict__ src, boo
                 const int r = (t >> 4) + 16 * i, w = t & 15;
                 const uint64_t word = (uint64_t)(m20 + (uint32_t)r) * win + a0 + (uint32_t)w;
                 const uint64_t x0 = 32ull * word;
-                v[i] = (act && (seed || x0 <= g.h)) ? ld_in(src + word, hostin) : 0u;
+                v[i] = (act && (seed || x0 <= g.h)) ? ld_in(src + (word & wmask), hostin) : 0u;
             }
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
@@ -145,7 +149,7 @@ __device__ __noinline__ void lane_bit_rows(const uint32_t* __restrict__ src, boo
             else if (x0 > g.h) v = 0u;
             else v = ld_in(src + (x0 >> 5), hostin) & ~(0xFFFFFFFFu >> (uint32_t)(g.h - x0 + 1));
         } else if (!placed) {
-            v = ld_in(src + (x0 >> 5), hostin);
+            v = ld_in(src + ((x0 >> 5) & wmask), hostin);
         } else {
             v = 0u;
             for (int b = 0; b < 32; ++b) {

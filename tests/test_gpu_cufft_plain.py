@@ -1,4 +1,6 @@
-"""The engine against the reference's plain cuFFT pipeline (baseline/cufft_plain.cu) on the same inputs.
+"""The engine against the reference's plain cuFFT pipeline (baseline/cufft_plain.cu) on the same inputs,
+with the pipeline's restated kernels and with the reference's own kernels (compiled from
+PrivacyAmplification.cu into baseline/_ref_cuda/ by baseline/ref_cuda.py).
 
 Both must equal the oracle where the oracle finishes quickly; at n = 2^27 the engine's output must be
 SHA3-equal to the cuFFT pipeline's on identical inputs (the reference's own 2^27 golden files are not
@@ -74,4 +76,60 @@ def test_2p27_sha3_equal_to_plain_cufft(plain_lib, gpu_engine):
             assert cp.residual(v) < 0.25
             assert gpu_engine.last_stats.max_residual < 0.25
     finally:
+        cp.close()
+
+
+@pytest.fixture(scope="module")
+def ref_kernels(plain_lib):
+    from baseline import ref_cuda
+    fb = ref_cuda.fatbin()
+    if fb is None:
+        pytest.skip("the reference's kernels were not compiled (its source tree was absent at build time)")
+    return fb
+
+
+@pytest.mark.parametrize("logn,do_xor,do_compress", [(16, True, True), (17, False, False), (20, False, True)])
+def test_reference_kernels_match_engine_and_oracle(plain_lib, ref_kernels, gpu_engine, logn, do_xor, do_compress):
+    """The reference's own binInt2float / correction / DC zero / product / ToBinaryArray[NoXOR] kernels with
+    cuFFT give the engine's bits and the oracle's, static seed over three blocks."""
+    n = 1 << logn
+    v = n // 4 + n // 8
+    flags = flags_of(do_xor, do_compress)
+    cp = plain_lib.CufftPlain(n, v)
+    cp.use_reference_kernels(ref_kernels)
+    seed, _ = O.random_block(n, v, 700 + logn)
+    try:
+        for blk in range(3):
+            _, recv = O.random_block(n, v, 1900 + 7 * logn + blk)
+            ks, kr = O.key_split(recv, n, v)
+            cp.load(seed=seed if blk == 0 else None, key_start=ks, key_rest=kr)
+            cp.process(recalc_seed=(blk == 0), do_xor=do_xor, do_compress=do_compress)
+            got = cp.output(pa.output_bytes(n, v, flags))
+            gpu_engine.set_seed(seed, n, -1)
+            assert np.array_equal(got, gpu_engine.process(ks, kr, n, v, flags)), blk
+            assert np.array_equal(got, O.ntt(seed, ks, kr, n, v, flags)), blk
+    finally:
+        cp.use_restated_kernels()
+        cp.close()
+
+
+def test_2p27_sha3_equal_to_reference_kernels(plain_lib, ref_kernels, gpu_engine):
+    """The bench's n = 2^27 inputs: the engine's output SHA3-equal to the reference's own kernels + cuFFT."""
+    n, v = 1 << 27, 50331648
+    seed, _ = O.random_block(n, v, 0x5EED)
+    cp = plain_lib.CufftPlain(n, v)
+    cp.use_reference_kernels(ref_kernels)
+    try:
+        gpu_engine.set_seed(seed, n, -1)
+        cp.load(seed=seed)
+        for blk in range(2):
+            _, recv = O.random_block(n, v, 0x5EED + 1 + blk)
+            ks, kr = O.key_split(recv, n, v)
+            cp.load(key_start=ks, key_rest=kr)
+            cp.process(recalc_seed=(blk == 0))
+            got = cp.output(v // 8)
+            mine = gpu_engine.process(ks, kr, n, v, DEFAULT)
+            assert O.sha3_256(got.tobytes()) == O.sha3_256(mine.tobytes()), blk
+    finally:
+        cp.use_restated_kernels()
         cp.close()

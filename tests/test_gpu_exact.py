@@ -173,3 +173,46 @@ def test_maximum_size_2p30(pa_lib):
     for r0 in (0, 64 * 1234567, v - 64):
         assert np.array_equal(np.unpackbits(out[r0 // 8: r0 // 8 + 8]), blk.rows(r0, r0 + 64) ^ krb[r0: r0 + 64]), r0
     blk.close()
+
+
+def structured_families(n, v):
+    """Inputs that concentrate the convolution's spectrum: runs of ones of several lengths, all ones,
+    periodic bit patterns and a single set bit, each with an all-ones and a random key."""
+    rng = np.random.default_rng(n + v)
+    words = n // 32
+    fams = {}
+    for frac in (2, 4, 8, 16):
+        s = np.zeros(words, np.uint32)
+        s[: words // frac] = 0xFFFFFFFF
+        fams["run_1/%d" % frac] = s
+    fams["ones"] = np.full(words, 0xFFFFFFFF, np.uint32)
+    fams["alt"] = np.full(words, 0xAAAAAAAA, np.uint32)
+    fams["bytes"] = np.full(words, 0xFF00FF00, np.uint32)
+    one = np.zeros(words, np.uint32)
+    one[0] = 0x80000000
+    fams["single"] = one
+    keys = {"ones": np.full(words + 1, 0xFFFFFFFF, np.uint32),
+            "random": rng.integers(0, 1 << 32, words + 1, dtype=np.uint64).astype(np.uint32)}
+    return fams, keys
+
+
+@pytest.mark.parametrize("logn", [10, 12, 14, 15])
+def test_single_cta_blocks_stay_within_fp32_budget(gpu_engine, logn):
+    """Blocks up to n = 2^15 run in one CTA (the path pa_process_noalloc uses, which has no guard): over
+    structured inputs that concentrate the spectrum, the FP32 residual stays below half the 0.25 guard and
+    every output is exact."""
+    n = 1 << logn
+    v = n // 4 + n // 8
+    fams, keys = structured_families(n, v)
+    worst = 0.0
+    for fname, seed in fams.items():
+        for kname, recv in keys.items():
+            ks, kr = O.key_split(recv, n, v)
+            gpu_engine.set_seed(seed, n, -1)
+            out = gpu_engine.process(ks, kr, n, v)
+            st = gpu_engine.last_stats
+            assert st.exact == 0, (fname, kname, st.max_residual)
+            worst = max(worst, st.max_residual)
+            assert np.array_equal(out, O.direct(seed, ks, kr, n, v)), (fname, kname)
+    print("n=2^%d worst residual %.4f" % (logn, worst))
+    assert worst < 0.125, worst
