@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -175,10 +176,14 @@ CP_API int cp_create(uint32_t n, uint32_t v, void** out) {
         destroy(p);
         return rc;
     };
-    if (cudaMalloc(&p->di1, (size_t)n * sizeof(float)) != cudaSuccess) return fail(-2);
+    // the reference's buffer sizes (PrivacyAmplification.cu:1572-1592): its kernels write past the n/2 + 1
+    // spectrum bins (ElementWiseProduct has no bounds check; its grid is rounded up to 1024 threads)
+    const size_t di1_floats = 2 * (((size_t)n + 992) / 2 + 1);
+    if (cudaMalloc(&p->di1, di1_floats * sizeof(float)) != cudaSuccess) return fail(-2);
     if (cudaMalloc(&p->di2, ((size_t)n + 992) * sizeof(float)) != cudaSuccess) return fail(-2);
-    if (cudaMalloc(&p->do1, ((size_t)n / 2 + 1) * sizeof(float2)) != cudaSuccess) return fail(-2);
-    if (cudaMalloc(&p->do2, ((size_t)n / 2 + 1) * sizeof(float2)) != cudaSuccess) return fail(-2);
+    if (cudaMalloc(&p->do1, (size_t)n * sizeof(float2)) != cudaSuccess) return fail(-2);
+    if (cudaMalloc(&p->do2, std::max((size_t)n * sizeof(float2), ((size_t)n + 992) * sizeof(float))) != cudaSuccess)
+        return fail(-2);
     if (cudaMalloc(&p->cnt, 2 * sizeof(uint32_t)) != cudaSuccess) return fail(-2);
     if (cudaMalloc(&p->corr, sizeof(float)) != cudaSuccess) return fail(-2);
     if (cudaMalloc(&p->resid, sizeof(float)) != cudaSuccess) return fail(-2);
@@ -190,7 +195,7 @@ CP_API int cp_create(uint32_t n, uint32_t v, void** out) {
     std::memset(p->h_seed, 0, words * 4);
     std::memset(p->h_ks, 0, words * 4);
     std::memset(p->h_kr, 0, (words + 31) * 4);
-    if (cudaMemset(p->di1, 0, (size_t)n * sizeof(float)) != cudaSuccess) return fail(-2);
+    if (cudaMemset(p->di1, 0, di1_floats * sizeof(float)) != cudaSuccess) return fail(-2);
     if (cudaMemset(p->di2, 0, ((size_t)n + 992) * sizeof(float)) != cudaSuccess) return fail(-2);
     if (cufftPlan1d(&p->fwd, (int)n, CUFFT_R2C, 1) != CUFFT_SUCCESS) return fail(-3);
     if (cufftPlan1d(&p->inv, (int)n, CUFFT_C2R, 1) != CUFFT_SUCCESS) return fail(-3);
