@@ -114,6 +114,7 @@ struct ServeLoop {
     cudaStream_t s = nullptr;
     cudaEvent_t ended = nullptr;  // recorded after each launch of the loop
     bool launched = false;
+    bool failed = false;  // a launch of the loop ended with a lane error or a request it took unfinished
     uint64_t next_ticket = 0;
     std::vector<uint64_t> owner;  // per ring slot: the ticket in it, or ~0 when free
     std::vector<pa_job> jobs;     // per ring slot: the request as submitted (exact recompute)
@@ -665,10 +666,31 @@ void free_serve(Pool* p) {
     p->serve = nullptr;
 }
 
-// (Re)launches the serving loop on the lanes; `claimed` keeps counting across launches.
+// Whether the last launch of the loop left a lane error word set (a bounded wait expired).
+int serve_lane_error(pa_engine* e, Pool* p, bool* any) {
+    std::vector<int> lerr(p->lanes->lanes);
+    PA_CUDA(e, cudaMemcpy(lerr.data(), p->lanes->ctl + 1 + 2 * p->lanes->lanes, lerr.size() * sizeof(int),
+                          cudaMemcpyDeviceToHost));
+    *any = false;
+    for (int x : lerr) *any = *any || x != 0;
+    return PA_OK;
+}
+
+// (Re)launches the serving loop on the lanes; `claimed` keeps counting across launches.  A loop whose last
+// launch ended with a lane error is not launched again: it stays failed until pa_serve_stop.
 int serve_launch(pa_engine* e, Pool* p) {
     ServeLoop* sv = p->serve;
     LaneSet* ls = p->lanes;
+    if (sv->launched) {
+        bool bad = false;
+        int rc = serve_lane_error(e, p, &bad);
+        if (rc) return rc;
+        if (bad) sv->failed = true;
+    }
+    if (sv->failed) {
+        e->last_cuda = (int)cudaErrorLaunchTimeout;
+        return PA_ERR_CUDA;
+    }
     PA_CUDA(e, cudaMemsetAsync(ls->ctl, 0, (1 + 3 * (size_t)ls->lanes) * sizeof(unsigned int), sv->s));
     pa::LaneArgs a = lane_args(ls, nullptr, 0);
     a.serve = 1;
@@ -1243,8 +1265,9 @@ int pa_serve_start(pa_engine* e, int32_t ctas_per_lane, uint32_t max_np, int32_t
     if (err == cudaSuccess) err = cudaHostGetDevicePointer((void**)&sv->d_ring, sv->ring, 0);
     if (err == cudaSuccess) err = cudaHostGetDevicePointer((void**)&sv->d_ctl, sv->ctl, 0);
     if (err == cudaSuccess) err = cudaMalloc(&sv->claimed, sizeof(unsigned long long));
-    if (err == cudaSuccess) err = cudaMalloc(&sv->lane_job, (size_t)ls->lanes * sizeof(pa::LaneJob));
-    if (err == cudaSuccess) err = cudaMalloc(&sv->lane_stats, (size_t)ls->lanes * 4 * sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaMalloc(&sv->lane_job, 2 * (size_t)ls->lanes * sizeof(pa::LaneJob));
+    if (err == cudaSuccess)
+        err = cudaMalloc(&sv->lane_stats, 2 * (size_t)ls->lanes * 4 * sizeof(unsigned long long));
     if (err == cudaSuccess) err = cudaMemset(sv->claimed, 0, sizeof(unsigned long long));
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaEventCreateWithFlags(&sv->ended, cudaEventDisableTiming);
@@ -1279,6 +1302,10 @@ int pa_serve_submit(pa_engine* e, const pa_job* job, uint64_t* ticket) {
     if (rc) return rc;
     if (lg.log_np > ls->cap) return PA_ERR_TOO_LARGE;
     if (reinterpret_cast<uintptr_t>(job->out) & 3u) return PA_ERR_INVALID_ARG;
+    if (sv->failed) {
+        e->last_cuda = (int)cudaErrorLaunchTimeout;
+        return PA_ERR_CUDA;
+    }
     const uint32_t k = (uint32_t)(sv->next_ticket % sv->size);
     if (sv->owner[k] != ~0ull) return PA_ERR_BUSY;  // the ring is full: collect with pa_serve_poll
     pa::LaneJob j{};
@@ -1328,17 +1355,21 @@ int pa_serve_poll(pa_engine* e, uint64_t ticket, pa_stats* stats) {
         PA_CUDA(e, cudaSetDevice(e->device));
         cudaError_t q = cudaEventQuery(sv->ended);
         if (q != cudaSuccess && q != cudaErrorNotReady) return cuda_fail(e, q);
-        std::vector<int> lerr(p->lanes->lanes);
-        PA_CUDA(e, cudaMemcpy(lerr.data(), p->lanes->ctl + 1 + 2 * p->lanes->lanes, lerr.size() * sizeof(int),
-                              cudaMemcpyDeviceToHost));
-        for (int x : lerr)
-            if (x) {  // a bounded wait of the loop expired: this request will not complete
-                sv->owner[k] = ~0ull;
-                e->last_cuda = (int)cudaErrorLaunchTimeout;
-                return PA_ERR_CUDA;
-            }
         if (__atomic_load_n(&slot->done, __ATOMIC_ACQUIRE) == ticket + 1ull) return PA_PENDING;  // just finished
-        int rc = serve_launch(e, p);  // the loop ended idle before this request was published
+        // the loop has ended without completing this request: a lane error, or a request it took and did
+        // not finish, means the request is lost; otherwise it was published after the loop ended idle
+        bool bad = false;
+        int rc = serve_lane_error(e, p, &bad);
+        if (rc) return rc;
+        unsigned long long claimed = 0;
+        PA_CUDA(e, cudaMemcpy(&claimed, sv->claimed, sizeof(claimed), cudaMemcpyDeviceToHost));
+        if (bad || sv->failed || ticket < claimed) {
+            sv->failed = true;
+            sv->owner[k] = ~0ull;
+            e->last_cuda = (int)cudaErrorLaunchTimeout;
+            return PA_ERR_CUDA;
+        }
+        rc = serve_launch(e, p);
         return rc ? rc : PA_PENDING;
     }
     if (slot->err) {

@@ -340,9 +340,12 @@ __device__ __forceinline__ int batch_claim(const LaneArgs& a, int lane) {
 }
 
 // Serving loop: the next published request (ticket) not yet taken by any lane; its descriptor is copied
-// from the host ring into the lane's device slot with the lane's counters.  With nothing published the
-// lane idles (a short sleep), and it ends when the host asks it to or after idle_ns without a request.
-__device__ __forceinline__ int serve_claim(const LaneArgs& a, int lane, unsigned long long& idle_since) {
+// from the host ring into the lane's device slot `buf` (two per lane, used in turn) with its counters,
+// and `buf` is returned.  Two slots, because rank 0 takes the next request before the lane barrier, while
+// the lane's other CTAs may still be finishing the previous request from the other slot and before that
+// request's completion is published from it.  With nothing published the lane idles (a short sleep),
+// and it ends when the host asks it to or after idle_ns without a request.
+__device__ __forceinline__ int serve_claim(const LaneArgs& a, int lane, int buf, unsigned long long& idle_since) {
     if (ld_volatile(a.err + lane)) return kLaneExit;
     const unsigned long long tail = ld_acquire_sys_u64(&a.host->tail);
     for (;;) {
@@ -369,7 +372,7 @@ __device__ __forceinline__ int serve_claim(const LaneArgs& a, int lane, unsigned
         j.g.seed_direct = src->g.seed_direct;
         j.g.exact_only = src->g.exact_only;
         j.flags = src->flags;
-        unsigned long long* st = a.lane_stats + 4 * lane;
+        unsigned long long* st = a.lane_stats + 4 * (2 * lane + buf);
         j.cnt = st;
         j.resid = reinterpret_cast<unsigned int*>(st + 2);
         j.pad_ = 0;
@@ -377,9 +380,9 @@ __device__ __forceinline__ int serve_claim(const LaneArgs& a, int lane, unsigned
         st[1] = j.seed_cnt ? *j.seed_cnt : 0ull;
         st[2] = 0ull;
         st[3] = c;  // the ticket, for the completion
-        a.lane_job[lane] = j;
+        a.lane_job[2 * lane + buf] = j;
         idle_since = 0;
-        return 0;
+        return buf;
     }
     if (*reinterpret_cast<volatile int*>(&a.host->stop)) return kLaneExit;
     const unsigned long long now = global_ns();
@@ -389,10 +392,11 @@ __device__ __forceinline__ int serve_claim(const LaneArgs& a, int lane, unsigned
     return kLaneIdle;
 }
 
-// Completion of the lane's last request, once every CTA of the lane has passed the barrier after its
-// finish stage: statistics into the host slot, then done = ticket + 1 (release at system scope).
-__device__ __forceinline__ void serve_publish(const LaneArgs& a, int lane) {
-    const unsigned long long* st = a.lane_stats + 4 * lane;
+// Completion of the lane's last request (device slot buf), once every CTA of the lane has passed the
+// barrier after its finish stage: statistics into the host slot, then done = ticket + 1 (release at system
+// scope).
+__device__ __forceinline__ void serve_publish(const LaneArgs& a, int lane, int buf) {
+    const unsigned long long* st = a.lane_stats + 4 * (2 * lane + buf);
     const unsigned long long tk = st[3];
     ServeSlot* s = a.ring + (tk % a.ring_size);
     volatile ServeSlot* vs = s;
@@ -413,23 +417,27 @@ __global__ void __launch_bounds__(kLaneThreads, 1) k_lanes(const __grid_constant
     __shared__ int s_job;
     unsigned int target = 0;
     unsigned long long idle_since = 0;
-    bool served = false;  // a request of this lane waits for its completion to be published
+    int served = -1;  // serving: the device slot of this lane's request whose completion is not yet published
+    int next_buf = 0;
     for (;;) {
         if (rank == 0 && threadIdx.x == 0) {
-            const int j = a.serve ? serve_claim(a, lane, idle_since) : batch_claim(a, lane);
+            const int j = a.serve ? serve_claim(a, lane, next_buf, idle_since) : batch_claim(a, lane);
             *reinterpret_cast<volatile int*>(a.slot + lane) = j;
         }
         const bool ok = lane_sync(a, lane, target);
-        if (served && rank == 0 && threadIdx.x == 0) serve_publish(a, lane);
-        served = false;
+        if (served >= 0 && rank == 0 && threadIdx.x == 0) serve_publish(a, lane, served);
+        served = -1;
         if (!ok) break;
         if (threadIdx.x == 0) s_job = ld_volatile(a.slot + lane);
         __syncthreads();
         const int j = s_job;
         if (j == kLaneIdle) continue;
         if (j < 0) break;
-        if (!lane_block(a, a.serve ? a.lane_job[lane] : a.jobs[j], a.serve != 0, lane, rank, target)) break;
-        served = a.serve != 0;
+        if (!lane_block(a, a.serve ? a.lane_job[2 * lane + j] : a.jobs[j], a.serve != 0, lane, rank, target)) break;
+        if (a.serve) {
+            served = j;
+            next_buf = j ^ 1;
+        }
     }
 }
 

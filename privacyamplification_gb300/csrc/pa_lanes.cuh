@@ -90,8 +90,8 @@ struct LaneArgs {
     uint32_t ring_size;
     ServeCtl* host;                  // host memory
     unsigned long long* claimed;     // device: tickets taken so far
-    LaneJob* lane_job;               // device, per lane: the request being served
-    unsigned long long* lane_stats;  // device, per lane: cnt[2], resid word
+    LaneJob* lane_job;               // device, two per lane (used in turn): requests being served
+    unsigned long long* lane_stats;  // device, two per lane: cnt[2], resid word, ticket
     unsigned long long idle_ns;      // time without a request after which the loop ends by itself
 };
 

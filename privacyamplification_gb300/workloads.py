@@ -256,10 +256,12 @@ def serve(engine, reqs, banks, out_slots=24, keep=lambda r: False, seed_ids=None
     return res
 
 
-def serve_device(engine, reqs, banks, out_slots=24, keep=lambda r: False, seed_ids=None, idle_sleep=20e-6):
+def serve_device(engine, reqs, banks, out_slots=24, keep=lambda r: False, seed_ids=None, idle_sleep=20e-6,
+                 stall_s=60.0):
     """Serves `reqs` in real time through the device-resident loop (engine.serve_start() first); returns
     latencies and the outputs of requests `keep` selects.  Admission is FIFO: a request waits for a free
-    pinned output buffer and a free ring slot; the device takes published requests as lanes free up."""
+    pinned output buffer and a free ring slot; the device takes published requests as lanes free up.
+    Raises TimeoutError when no request completes for stall_s seconds."""
     import torch
     max_out = max(output_bytes(r.n, r.v, r.flags) for r in reqs)
     outs = [torch.empty(max_out + 4, dtype=torch.uint8).pin_memory().numpy() for _ in range(out_slots)]
@@ -270,8 +272,11 @@ def serve_device(engine, reqs, banks, out_slots=24, keep=lambda r: False, seed_i
     res = ServeResult(latency_ms=[], wall_s=0.0, bits=0)
     t0 = time.perf_counter()
     remaining = len(reqs)
+    last_done = t0
     while remaining:
         now = time.perf_counter() - t0
+        if inflight and time.perf_counter() - last_done > stall_s:
+            raise TimeoutError("the serving loop completed no request in %.0f s" % stall_s)
         progressed = False
         while pending and pending[0].arrival <= now:
             waiting.append(pending.popleft())
@@ -295,6 +300,7 @@ def serve_device(engine, reqs, banks, out_slots=24, keep=lambda r: False, seed_i
                 continue
             r, ob = inflight.pop(t)
             r.done = time.perf_counter() - t0
+            last_done = time.perf_counter()
             r.exact = st.exact
             res.exact += st.exact
             res.latency_ms.append((r.done - r.arrival) * 1e3)

@@ -45,6 +45,20 @@ def test_overlapping_requests_match_oracle(torch_cuda):
         assert np.array_equal(res.outputs[r.rid], oracle_of(banks, r)), r
 
 
+def test_requests_queued_behind_busy_lanes(torch_cuda):
+    """Every request arrives at once and two lanes serve 24 of them, so a lane takes its next request
+    while its other CTAs still finish the previous one: each completion is published for its own request."""
+    reqs = W.poisson_requests(rate=1e7, count=24, lo=16, hi=23, rng_seed=0x5E3)
+    words = max(r.n // 32 + max(r.seed_word0, r.key_word0) for r in reqs) + 64
+    banks = W.HostBanks(words)
+    with pa.Engine(max_sample_size=1 << 23) as eng:
+        assert eng.serve_start(ctas_per_lane=76, max_np=1 << 23, ring_slots=32) == 2
+        res = W.serve_device(eng, reqs, banks, out_slots=24, keep=lambda r: True, stall_s=30.0)
+        eng.serve_stop()
+    for r in reqs:
+        assert np.array_equal(res.outputs[r.rid], oracle_of(banks, r)), r
+
+
 def test_static_seeds_served(torch_cuda):
     """Static seeds (spectra cached before the loop starts), powers of two from 2^16 to 2^22."""
     reqs = W.poisson_requests(rate=3000, count=20, lo=16, hi=22, static=True, rng_seed=0x5E2)
@@ -134,7 +148,7 @@ def test_config5_draw_device_loop(torch_cuda):
     banks = W.HostBanks(words)
     with pa.Engine(max_sample_size=1 << 27) as eng:
         eng.serve_start(ctas_per_lane=38, max_np=1 << 27)
-        res = W.serve_device(eng, reqs, banks, out_slots=8, keep=lambda r: True)
+        res = W.serve_device(eng, reqs, banks, out_slots=8, keep=lambda r: True, stall_s=60.0)
         eng.serve_stop()
     for r in reqs:
         assert np.array_equal(res.outputs[r.rid], oracle_of(banks, r)), r
