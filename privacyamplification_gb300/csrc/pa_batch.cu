@@ -111,6 +111,8 @@ struct ServeLoop {
     unsigned long long* claimed = nullptr;  // device
     pa::LaneJob* lane_job = nullptr;        // device
     unsigned long long* lane_stats = nullptr;
+    uint32_t* stage = nullptr;  // device: per lane, a request's inputs copied from host memory
+    size_t stage_stride = 0;
     cudaStream_t s = nullptr;
     cudaEvent_t ended = nullptr;  // recorded after each launch of the loop
     bool launched = false;
@@ -660,6 +662,7 @@ void free_serve(Pool* p) {
     cudaFree(sv->claimed);
     cudaFree(sv->lane_job);
     cudaFree(sv->lane_stats);
+    cudaFree(sv->stage);
     if (sv->ended) cudaEventDestroy(sv->ended);
     if (sv->s) cudaStreamDestroy(sv->s);
     delete sv;
@@ -700,6 +703,8 @@ int serve_launch(pa_engine* e, Pool* p) {
     a.claimed = sv->claimed;
     a.lane_job = sv->lane_job;
     a.lane_stats = sv->lane_stats;
+    a.stage = sv->stage;
+    a.stage_stride = sv->stage_stride;
     a.idle_ns = sv->idle_ns;
     int rc = pa::launch_lanes(a, ls->lanes * ls->T, ls->smem, sv->s);
     if (rc) return cuda_fail(e, (cudaError_t)rc);
@@ -1268,6 +1273,8 @@ int pa_serve_start(pa_engine* e, int32_t ctas_per_lane, uint32_t max_np, int32_t
     if (err == cudaSuccess) err = cudaMalloc(&sv->lane_job, 2 * (size_t)ls->lanes * sizeof(pa::LaneJob));
     if (err == cudaSuccess)
         err = cudaMalloc(&sv->lane_stats, 2 * (size_t)ls->lanes * 4 * sizeof(unsigned long long));
+    sv->stage_stride = 3 * ((size_t(1) << ls->cap) / 32 + 64);
+    if (err == cudaSuccess) err = cudaMalloc(&sv->stage, (size_t)ls->lanes * sv->stage_stride * sizeof(uint32_t));
     if (err == cudaSuccess) err = cudaMemset(sv->claimed, 0, sizeof(unsigned long long));
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&sv->s, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaEventCreateWithFlags(&sv->ended, cudaEventDisableTiming);

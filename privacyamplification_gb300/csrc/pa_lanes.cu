@@ -291,8 +291,30 @@ __device__ __forceinline__ void lane_pass_b(bool seed, const CUtensorMap* mapY, 
 }
 
 // One block on one lane.  Returns false when a lane barrier failed (the lane's error word is set).
-__device__ __forceinline__ bool lane_block(const LaneArgs& a, const LaneJob& j, bool hostin, int lane, int rank,
+// Copies `words` words from host memory into the lane's device staging, the lane's CTAs taking
+// interleaved runs of 512 consecutive words (coalesced loads that bypass the caches; the host may have
+// rewritten the buffer since an earlier request).
+__device__ __noinline__ void lane_stage_in(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, size_t words,
+                                           uint32_t first, uint32_t stride) {
+    const size_t step = (size_t)stride * kLaneThreads * 4;
+    for (size_t base = (size_t)first * kLaneThreads * 4 + threadIdx.x; base < words; base += step) {
+        uint32_t v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t i = base + (size_t)u * kLaneThreads;
+            v[u] = i < words ? __ldcv(src + i) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const size_t i = base + (size_t)u * kLaneThreads;
+            if (i < words) dst[i] = v[u];
+        }
+    }
+}
+
+__device__ __forceinline__ bool lane_block(const LaneArgs& a, const LaneJob& jin, bool hostin, int lane, int rank,
                                            unsigned int& target) {
+    LaneJob j = jin;
     const BlockGeom g = j.g;
     float2* Y = a.work + (size_t)lane * a.work_stride;
     float2* Z = a.work2 + (size_t)lane * a.work_stride;
@@ -301,6 +323,18 @@ __device__ __forceinline__ bool lane_block(const LaneArgs& a, const LaneJob& j, 
     const CUtensorMap* maps = a.maps + ((size_t)lane * kLaneMaps + (size_t)mi) * 2;
     int* err = a.err + lane;
     const uint32_t first = (uint32_t)rank, stride = (uint32_t)a.T;
+    if (hostin) {  // a served request: its inputs move to the lane's device staging first, in one pass
+        uint32_t* st = a.stage + (size_t)lane * a.stage_stride;
+        const size_t wn = g.n / 32u, wh = g.h / 32u + 1u, wv = g.v / 32u;
+        lane_stage_in(j.key_start, st, wh, first, stride);
+        if (j.seed) lane_stage_in(j.seed, st + wn, wn, first, stride);
+        if (j.key_rest) lane_stage_in(j.key_rest, st + 2 * wn, wv, first, stride);
+        j.key_start = st;
+        if (j.seed) j.seed = st + wn;
+        if (j.key_rest) j.key_rest = st + 2 * wn;
+        hostin = false;  // the output is still written to host memory directly
+        if (!lane_sync(a, lane, target)) return false;
+    }
     float2* spec = const_cast<float2*>(j.spec);
     // phase 0: the block's own seed (bit rows, pass A, pass B into its spectrum); phase 1: the key
     for (int phase = j.seed ? 0 : 1; phase < 2; ++phase) {

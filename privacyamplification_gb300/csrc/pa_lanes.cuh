@@ -93,6 +93,8 @@ struct LaneArgs {
     LaneJob* lane_job;               // device, two per lane (used in turn): requests being served
     unsigned long long* lane_stats;  // device, two per lane: cnt[2], resid word, ticket
     unsigned long long idle_ns;      // time without a request after which the loop ends by itself
+    uint32_t* stage;                 // device, per lane: a served request's key_start, seed, key_rest
+    size_t stage_stride;             // words per lane (3 * (Np / 32) for the largest Np)
 };
 
 // Host side (pa_lanes.cu).
