@@ -279,9 +279,10 @@ def dist_setup():
 
 
 def run_reference(args):
-    """The reference arm: the reference ships no CPU implementation of the path and its CUDA build is not
-    on the GPU host, so this times the CPU port (oracle, exact NTT, all host threads) on the same workload,
-    one whole block per step.  Under torchrun only rank 0 runs it."""
+    """The reference arm, on the host cores: the reference ships no CPU implementation of the path, so this
+    times the CPU port (oracle, exact NTT, all host threads) on the same workload, one whole block per
+    step.  The reference's own CUDA kernels on the GPU are timed by the engine arm (`reference_cuda`).
+    Under torchrun only rank 0 runs it."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
