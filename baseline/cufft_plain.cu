@@ -334,6 +334,202 @@ CP_API int cp_residual(void* h, uint32_t out_bits, float* max_resid) {
     return 0;
 }
 
+// ============================================================================ sub-block bank
+// The reference's sub-block variant (PrivacyAmplification/PrivacyAmplification_subblocks.cu): a bank of
+// 2^27 bits cut into B = 2^27 / s sub-blocks of s bits (:1006-1031; its speedtest sweeps s = 2^10..2^27
+// with v = s/4 + s/8, :1210-1236), every step one launch over the whole bank and the transforms one
+// batched cuFFT plan per direction (cufftPlan1d(s, R2C / C2R, B), :1058-1081).  Each sub-block is an
+// ordinary block with its own seed, key and counts, so the restatement here keeps the per-sub-block
+// counts, corrections and DC bins (the reference file's own kernels do not: it is not built by any of
+// its Makefiles).  Unlike cp_process, the bank runs from device memory with no host sync between steps,
+// and is timed with CUDA events: the strongest form of the batched-cuFFT design, to hold the engine's
+// batch of equal blocks against.
+namespace {
+
+struct Bank {
+    uint32_t s = 0, v = 0, B = 0, log_s = 0;
+    cufftHandle fwd = 0, inv = 0;
+    uint32_t *seed = nullptr, *ks = nullptr, *kr = nullptr, *out = nullptr;  // device words
+    float *di1 = nullptr, *di2 = nullptr;
+    float2 *do1 = nullptr, *do2 = nullptr;
+    uint32_t* cnt = nullptr;  // [0, B) seed ones, [B, 2B) key ones
+    float* corr = nullptr;    // B
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    bool seed_ready = false;
+};
+
+// One thread per bit of the bank, 1024 bits per CUDA block (s >= 1024: a CUDA block never straddles
+// two sub-blocks); a set bit stores h1 and adds 1 to its sub-block's counter.
+__global__ void k_unpack_bank(const uint32_t* __restrict__ words, float* __restrict__ out, uint32_t* ones,
+                              uint32_t log_s) {
+    __shared__ uint32_t w[32];
+    const uint32_t t = threadIdx.x;
+    const size_t base = (size_t)blockIdx.x * 1024u;
+    if (t < 32) w[t] = words[base / 32u + t];
+    __syncthreads();
+    const uint32_t bit = (w[t >> 5] >> (31u - (t & 31u))) & 1u;
+    if (bit) atomicAdd(ones + (base >> log_s), 1u);
+    out[base + t] = bit ? kH1 : 0.0f;
+}
+
+__global__ void k_correction_bank(const uint32_t* cnt, float* corr, uint32_t B, uint32_t s) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B) return;
+    const uint32_t prod = cnt[i] * cnt[B + i];
+    corr[i] = (float)fmod((double)prod / (double)s, 2.0);
+}
+
+__global__ void k_zero_dc_bank(float2* a, float2* b, uint32_t B, uint32_t dist) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B) return;
+    a[(size_t)i * dist] = make_float2(0.f, 0.f);
+    b[(size_t)i * dist] = make_float2(0.f, 0.f);
+}
+
+__global__ void k_product_bank(float2* __restrict__ key, const float2* __restrict__ seed, size_t count) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float2 a = key[i], b = seed[i];
+    const float ax = a.x / kR, ay = a.y / kR, bx = b.x / kR, by = b.y / kR;
+    key[i] = make_float2(ax * bx - ay * by, ax * by + ay * bx);
+}
+
+// One thread per output bit: rint(x / norm + corr) & 1, a warp's 32 bits gathered by ballot into one
+// word in the reference's byte order (bit k at byte k/8, bit 7 - k%8), XORed with key_rest in the same
+// layout.  Grid: (v/32 words per sub-block / 8 warps, B).
+template <bool XOR>
+__global__ void k_pack_bank(const float* __restrict__ inv, uint32_t* __restrict__ out,
+                            const uint32_t* __restrict__ key_rest, const float* corr, uint32_t s, uint32_t v,
+                            float norm) {
+    const uint32_t i = blockIdx.y, words = v / 32u;
+    const uint32_t word = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
+    if (word >= words) return;  // whole warps
+    const uint32_t lane = threadIdx.x & 31u;
+    const float x = inv[(size_t)i * s + word * 32u + lane] / norm + corr[i];
+    const uint32_t bits = __ballot_sync(0xffffffffu, ((uint32_t)__float2int_rn(x) & 1u) != 0u);
+    if (lane == 0) {
+        uint32_t w = __byte_perm(__brev(bits), 0, 0x0123);
+        if (XOR) w ^= __byte_perm(key_rest[(size_t)i * words + word], 0, 0x0123);
+        out[(size_t)i * words + word] = w;
+    }
+}
+
+void destroy_bank(Bank* b) {
+    if (!b) return;
+    if (b->fwd) cufftDestroy(b->fwd);
+    if (b->inv) cufftDestroy(b->inv);
+    cudaFree(b->seed);
+    cudaFree(b->ks);
+    cudaFree(b->kr);
+    cudaFree(b->out);
+    cudaFree(b->di1);
+    cudaFree(b->di2);
+    cudaFree(b->do1);
+    cudaFree(b->do2);
+    cudaFree(b->cnt);
+    cudaFree(b->corr);
+    for (cudaEvent_t e : b->ev)
+        if (e) cudaEventDestroy(e);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+}
+
+}  // namespace
+
+// s: power of two in [2^10, 2^27]; v: multiple of 32 below s; B sub-blocks (B * s <= 2^28).
+CP_API int cb_create(uint32_t s, uint32_t v, uint32_t B, void** out) {
+    if (!out || s < 1024u || s > (1u << 27) || (s & (s - 1u)) || (v & 31u) || v == 0 || v >= s || B == 0 ||
+        (uint64_t)B * s > (1ull << 28))
+        return -1;
+    Bank* b = new (std::nothrow) Bank;
+    if (!b) return -2;
+    b->s = s, b->v = v, b->B = B;
+    while ((1u << b->log_s) < s) ++b->log_s;
+    const size_t bits = (size_t)B * s, dist = s / 2u + 1u;
+    auto fail = [&](int rc) {
+        destroy_bank(b);
+        return rc;
+    };
+    if (cudaMalloc(&b->seed, bits / 8) != cudaSuccess || cudaMalloc(&b->ks, bits / 8) != cudaSuccess ||
+        cudaMalloc(&b->kr, (size_t)B * v / 8) != cudaSuccess || cudaMalloc(&b->out, (size_t)B * v / 8) != cudaSuccess ||
+        cudaMalloc(&b->di1, bits * sizeof(float)) != cudaSuccess || cudaMalloc(&b->di2, bits * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&b->do1, B * dist * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&b->do2, B * dist * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&b->cnt, 2 * (size_t)B * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&b->corr, (size_t)B * sizeof(float)) != cudaSuccess)
+        return fail(-2);
+    if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev[0]) != cudaSuccess || cudaEventCreate(&b->ev[1]) != cudaSuccess)
+        return fail(-2);
+    if (cudaMemset(b->seed, 0, bits / 8) != cudaSuccess || cudaMemset(b->ks, 0, bits / 8) != cudaSuccess ||
+        cudaMemset(b->kr, 0, (size_t)B * v / 8) != cudaSuccess)
+        return fail(-2);
+    if (cufftPlan1d(&b->fwd, (int)s, CUFFT_R2C, (int)B) != CUFFT_SUCCESS) return fail(-3);
+    if (cufftPlan1d(&b->inv, (int)s, CUFFT_C2R, (int)B) != CUFFT_SUCCESS) return fail(-3);
+    if (cufftSetStream(b->fwd, b->st) != CUFFT_SUCCESS || cufftSetStream(b->inv, b->st) != CUFFT_SUCCESS) return fail(-3);
+    if (cudaDeviceSynchronize() != cudaSuccess) return fail(-2);
+    *out = b;
+    return 0;
+}
+
+CP_API void cb_destroy(void* h) { destroy_bank(static_cast<Bank*>(h)); }
+
+// Host -> device copies of the bank's inputs: seed and key_start B * s/32 words (sub-block i at i * s/32,
+// key_start zero past bit h of each sub-block), key_rest B * v/32 words (null: keep).  Not timed.
+CP_API int cb_load(void* h, const uint32_t* seed, const uint32_t* key_start, const uint32_t* key_rest) {
+    Bank* b = static_cast<Bank*>(h);
+    const size_t bytes = (size_t)b->B * b->s / 8;
+    if (seed) {
+        CP_TRY(cudaMemcpy(b->seed, seed, bytes, cudaMemcpyHostToDevice));
+        b->seed_ready = false;
+    }
+    if (key_start) CP_TRY(cudaMemcpy(b->ks, key_start, bytes, cudaMemcpyHostToDevice));
+    if (key_rest) CP_TRY(cudaMemcpy(b->kr, key_rest, (size_t)b->B * b->v / 8, cudaMemcpyHostToDevice));
+    return 0;
+}
+
+// Queues one bank on the bank's stream between two events and waits for it; *ms = device time.
+// recalc_seed = 0 reuses the seed spectra (the first call always computes them).
+CP_API int cb_run(void* h, int recalc_seed, int do_xor, float* ms) {
+    Bank* b = static_cast<Bank*>(h);
+    const uint32_t s = b->s, B = b->B, dist = s / 2u + 1u;
+    const size_t bits = (size_t)B * s;
+    const bool seed = recalc_seed || !b->seed_ready;
+    cudaStream_t st = b->st;
+    CP_TRY(cudaEventRecord(b->ev[0], st));
+    if (seed) {
+        CP_TRY(cudaMemsetAsync(b->cnt, 0, (size_t)B * sizeof(uint32_t), st));
+        k_unpack_bank<<<(unsigned)(bits / 1024u), 1024, 0, st>>>(b->seed, b->di2, b->cnt, b->log_s);
+        CP_FFT(cufftExecR2C(b->fwd, b->di2, reinterpret_cast<cufftComplex*>(b->do2)));
+    }
+    CP_TRY(cudaMemsetAsync(b->cnt + B, 0, (size_t)B * sizeof(uint32_t), st));
+    k_unpack_bank<<<(unsigned)(bits / 1024u), 1024, 0, st>>>(b->ks, b->di1, b->cnt + B, b->log_s);
+    k_correction_bank<<<(B + 255u) / 256u, 256, 0, st>>>(b->cnt, b->corr, B, s);
+    CP_FFT(cufftExecR2C(b->fwd, b->di1, reinterpret_cast<cufftComplex*>(b->do1)));
+    k_zero_dc_bank<<<(B + 255u) / 256u, 256, 0, st>>>(b->do1, b->do2, B, dist);
+    const size_t count = (size_t)B * dist;
+    k_product_bank<<<(unsigned)((count + 255u) / 256u), 256, 0, st>>>(b->do1, b->do2, count);
+    CP_FFT(cufftExecC2R(b->inv, reinterpret_cast<cufftComplex*>(b->do1), b->di2));
+    const float norm = (float)s / (2048.0f * kR) / (2048.0f * kR);
+    const dim3 grid((b->v / 32u + 7u) / 8u, B);
+    if (do_xor) k_pack_bank<true><<<grid, 256, 0, st>>>(b->di2, b->out, b->kr, b->corr, s, b->v, norm);
+    else k_pack_bank<false><<<grid, 256, 0, st>>>(b->di2, b->out, nullptr, b->corr, s, b->v, norm);
+    CP_TRY(cudaGetLastError());
+    CP_TRY(cudaEventRecord(b->ev[1], st));
+    CP_TRY(cudaEventSynchronize(b->ev[1]));
+    if (seed) b->seed_ready = !recalc_seed;  // a static seed's spectra are kept; C2R overwrote its floats only
+    if (ms) CP_TRY(cudaEventElapsedTime(ms, b->ev[0], b->ev[1]));
+    return 0;
+}
+
+// Device -> host copy of the B * v/32 output words (sub-block i at i * v/32).
+CP_API int cb_output(void* h, uint32_t* out) {
+    Bank* b = static_cast<Bank*>(h);
+    CP_TRY(cudaMemcpy(out, b->out, (size_t)b->B * b->v / 8, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
 // Loads the reference's kernels from a fatbin built from PrivacyAmplification.cu (baseline/ref_cuda.py)
 // and sets their __constant__ values for blocks of n bits (PrivacyAmplification.cu:1597-1606, 1729-1732):
 // c0 = 0, h0 = 0, h1_reduced = 2^-11, sample_size = n, pre_mul_reduction = 2^5,

@@ -1,4 +1,5 @@
-"""GPU baseline: the reference's plain single-block cuFFT pipeline (cufft_plain.cu), built and bound here.
+"""GPU baselines: the reference's plain single-block cuFFT pipeline and its sub-block bank (batched cuFFT
+plans over equal sub-blocks), both in cufft_plain.cu, built and bound here.
 
     python -m baseline.cufft_plain          # build libcufft_plain.so in-tree
 
@@ -122,6 +123,74 @@ class CufftPlain:
     def close(self):
         if self._h:
             self._lib.cp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CufftBank:
+    """The sub-block bank (cb_*): B equal sub-blocks of s bits, one batched cuFFT plan per direction, device
+    inputs, device-timed."""
+
+    def __init__(self, s: int, v: int, B: int):
+        if not os.path.exists(LIB):
+            raise RuntimeError("%s not built: run `python -m baseline.cufft_plain`" % LIB)
+        lib = ctypes.CDLL(LIB)
+        vp, u32p = ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)
+        lib.cb_create.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(vp)]
+        lib.cb_create.restype = ctypes.c_int
+        lib.cb_destroy.argtypes = [vp]
+        lib.cb_destroy.restype = None
+        lib.cb_load.argtypes = [vp, u32p, u32p, u32p]
+        lib.cb_load.restype = ctypes.c_int
+        lib.cb_run.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+        lib.cb_run.restype = ctypes.c_int
+        lib.cb_output.argtypes = [vp, u32p]
+        lib.cb_output.restype = ctypes.c_int
+        self._lib, self.s, self.v, self.B = lib, s, v, B
+        h = vp()
+        rc = lib.cb_create(s, v, B, ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError("cb_create(%d, %d, %d) failed: %d" % (s, v, B, rc))
+        self._h = h
+
+    @staticmethod
+    def _ptr(a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, np.uint32)
+        return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+    def load(self, seed=None, key_start=None, key_rest=None):
+        """seed, key_start: (B, s/32) words; key_rest: (B, v/32) words (None: keep)."""
+        keep = [self._ptr(x) for x in (seed, key_start, key_rest)]
+        rc = self._lib.cb_load(self._h, *[k[1] if k else None for k in keep])
+        if rc != 0:
+            raise RuntimeError("cb_load failed: %d" % rc)
+
+    def run(self, recalc_seed: bool, do_xor: bool = True) -> float:
+        """One bank; returns its device time in ms."""
+        ms = ctypes.c_float()
+        rc = self._lib.cb_run(self._h, int(recalc_seed), int(do_xor), ctypes.byref(ms))
+        if rc != 0:
+            raise RuntimeError("cb_run failed: %d" % rc)
+        return ms.value
+
+    def outputs(self) -> np.ndarray:
+        """(B, v/8) output bytes."""
+        out = np.empty(self.B * self.v // 32, np.uint32)
+        rc = self._lib.cb_output(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        if rc != 0:
+            raise RuntimeError("cb_output failed: %d" % rc)
+        return out.view(np.uint8).reshape(self.B, self.v // 8)
+
+    def close(self):
+        if self._h:
+            self._lib.cb_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -132,9 +132,8 @@ class ClockSampler:
 
 
 def make_inputs(nkeys):
-    from oracle.oracle import random_block  # input generator only (seeded PRNG)
-    import numpy as np
     import privacyamplification_gb300 as pa
+    from privacyamplification_gb300.workloads import random_block
     seed, _ = random_block(N_BITS, V_BITS, 0x5EED)
     keys = []
     for i in range(nkeys):
@@ -590,7 +589,7 @@ def run_dynamic27(args):
     import numpy as np
     import torch
     import privacyamplification_gb300 as pa
-    from oracle.oracle import random_block
+    from privacyamplification_gb300.workloads import random_block
     pa.load_library()
     dev = torch.device("cuda", 0)
     eng = pa.Engine(max_sample_size=N_BITS)
@@ -728,6 +727,90 @@ def run_batch(args):
     eng.close()
 
 
+def run_banked(args):
+    """Equal sub-blocks of a 2^27-bit bank (the reference's sub-block variant): the engine's batch of B
+    equal blocks (one CUDA graph) against the bank on batched cuFFT plans, static and dynamic seeds."""
+    import privacyamplification_gb300 as pa
+    from privacyamplification_gb300 import workloads as W
+    from baseline import cufft_plain
+    pa.load_library()
+    cufft_plain.build()
+    sizes, total_bits, total_s = [], 0, 0.0
+    for log_s in (18, 20, 22, 25):
+        s, v, seeds, ks, kr = W.sub_block_bank(log_s)
+        B = seeds.shape[0]
+        bits = B * s
+        row = {"log_s": log_s, "sub_blocks": B, "v": v}
+        bank = cufft_plain.CufftBank(s, v, B)
+        bank.load(seeds, ks, kr)
+        eng = pa.Engine(max_sample_size=s)
+        try:
+            for static in (True, False):
+                tag = "static" if static else "dynamic"
+                for _ in range(args.warmup):
+                    bank.run(recalc_seed=not static)
+                with ClockSampler(0) as clk:
+                    ms = [bank.run(recalc_seed=not static) for _ in range(args.steps)]
+                row["cufft_bank_" + tag] = {"gbit_s": bits / (statistics.median(ms) / 1e3) / 1e9,
+                                            "ms_median": statistics.median(ms), "clocks": clk.summary()}
+                ref_out = bank.outputs()
+                db = W.DeviceBank(eng, s, v, seeds, ks, kr, static)
+                for _ in range(args.warmup):
+                    db.run(pa.BATCH_GRAPH)
+                with ClockSampler(0) as clk:
+                    sts = [db.run(pa.BATCH_GRAPH) for _ in range(args.steps)]
+                ms = [st[0].gpu_ms for st in sts]
+                mine = db.outputs()
+                row["engine_graph_" + tag] = {
+                    "gbit_s": bits / (statistics.median(ms) / 1e3) / 1e9, "ms_median": statistics.median(ms),
+                    "max_residual": max(x.max_residual for x in sts[-1]), "clocks": clk.summary(),
+                    "blocks_equal_cufft_bank": int(sum((mine[i] == ref_out[i]).all() for i in range(B)))}
+                row["engine_over_cufft_" + tag] = row["engine_graph_" + tag]["gbit_s"] / row["cufft_bank_" + tag]["gbit_s"]
+                # group sizes: one launch per pass for 2^20 .. 2^27 bits of the bank's blocks
+                if static:
+                    sweep = {}
+                    for lb in (20, 22, 24, 27):
+                        if lb <= log_s:
+                            continue
+                        eng.set_groups(0, lb)
+                        for _ in range(args.warmup):
+                            db.run(pa.BATCH_GRAPH)
+                        ms = [db.run(pa.BATCH_GRAPH)[0].gpu_ms for _ in range(args.steps)]
+                        sweep["2^%d" % lb] = bits / (statistics.median(ms) / 1e3) / 1e9
+                    eng.set_groups(0, 0)
+                    row["engine_group_bits_sweep_gbit_s"] = sweep
+                # the same bank launched block by block (no groups), and as one persistent lane launch
+                # (lanes hold cyclic lengths from 2^20)
+                alt = [("graph_no_group", pa.BATCH_GRAPH | pa.BATCH_NO_GROUP)]
+                if log_s >= 20:
+                    alt.append(("persistent", pa.BATCH_PERSISTENT))
+                for name, fl in alt:
+                    for _ in range(args.warmup):
+                        db.run(fl)
+                    sts = [db.run(fl) for _ in range(args.steps)]
+                    ms = [st[0].gpu_ms for st in sts]
+                    row["engine_%s_%s" % (name, tag)] = {
+                        "gbit_s": bits / (statistics.median(ms) / 1e3) / 1e9, "ms_median": statistics.median(ms),
+                        "blocks_equal_cufft_bank": int(sum((db.outputs()[i] == ref_out[i]).all() for i in range(B)))}
+                if static:
+                    total_bits += bits
+                    total_s += row["engine_graph_static"]["ms_median"] / 1e3
+                del db
+        finally:
+            eng.close()
+            bank.close()
+        sizes.append(row)
+    value = total_bits / total_s / 1e9
+    _line(METRIC, value, UNIT, args.steps, args.warmup, total_s / len(sizes) * 1e3,
+          "sub-block banks: 2^27 bits as B equal blocks of s = 2^18 / 2^20 / 2^22 / 2^25 bits (B = 512 / 128 / 32 / "
+          "4), v = 3s/8, each block with its own seed and key; value: the engine's static-seed banks (one "
+          "CUDA graph of the bank's groups: one launch per pass for up to 2^27 bits of equal blocks) over all "
+          "four sizes",
+          {"sizes": sizes, "baseline": "the reference's sub-block variant (PrivacyAmplification_subblocks.cu) "
+                                       "restated on batched cuFFT plans, device inputs, no host syncs "
+                                       "(baseline/cufft_plain.cu cb_*)"})
+
+
 def run_serve(args, static):
     """Poisson arrivals; p50/p99 latency and sustained Gbit/s per rate; sampled same-alone-vs-in-mix check."""
     import privacyamplification_gb300 as pa
@@ -816,7 +899,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT pipeline baseline leg")
     ap.add_argument("--workload", default="static27",
-                    choices=["static27", "dynamic27", "dynamic29", "exact29", "batch", "serve", "serve-static"],
+                    choices=["static27", "dynamic27", "dynamic29", "exact29", "batch", "banked", "serve", "serve-static"],
                     help="static27 (default): the headline line; the others print their own line")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -829,6 +912,8 @@ def main():
         return run_big29(args, force_exact=args.workload == "exact29")
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "banked":
+        return run_banked(args)
     if args.workload in ("serve", "serve-static"):
         return run_serve(args, static=args.workload == "serve-static")
     return run_ours(args)

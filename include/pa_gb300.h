@@ -129,6 +129,17 @@ PA_API int pa_last_cuda_error(pa_engine* e);
  * cudaErrorLaunchTimeout in pa_last_cuda_error).  The context stays usable afterwards. */
 PA_API int pa_selftest_wait_timeout(int32_t device_id, uint32_t rounds, int32_t* status);
 
+/* Measurement of one radix-16 DFT stage on the tensor cores against the FP32 butterflies (no counterpart
+ * in the reference, whose transforms are cuFFT calls, PrivacyAmplification.cu:1736,1745).  d_in / d_out
+ * hold `butterflies` (a multiple of 128) groups of 16 complex FP32 values, re/im interleaved, 16-byte
+ * aligned; each group gets `reps` forward 16-point DFTs, scaled by 1/256 after every fourth (so that
+ * reps % 4 == 0 returns the input).  method 0: FP32 butterflies in registers (the passes' stage);
+ * 1: tcgen05.mma kind::tf32 with operands split into TF32 high and low parts, three products (FP32-level
+ * accuracy); 2: one TF32 product.  ctas_per_sm: 1..16 for method 0, 1..4 for the tensor methods.  A
+ * bounded wait that expires stores 1 in *d_err (device int).  Queued on `stream`, not synchronised. */
+PA_API int pa_dft16_stages(const float* d_in, float* d_out, uint32_t butterflies, uint32_t reps, int32_t method,
+                           int32_t ctas_per_sm, int32_t* d_err, void* stream);
+
 /* ---- Batched and served blocks -------------------------------------------------------------------
  * No counterpart in the reference: its mainloop (PrivacyAmplification.cu:1686-2118) runs one block at
  * a time with a host sync after every step.  Here blocks of different sizes run concurrently on a pool
@@ -171,11 +182,20 @@ PA_API int pa_seed_cache_clear(pa_engine* e);
  * PA_BATCH_GRAPH: capture the whole batch as one CUDA graph the first time these exact jobs are seen
  * and replay it afterwards.  PA_BATCH_SERIAL: one slot, jobs in order (the per-block launch
  * sequence, for comparison).  pa_batch_sync waits, recomputes blocks over the residual limit
- * exactly, and fills stats[i] for job i (gpu_ms: the whole batch's device time). */
+ * exactly, and fills stats[i] for job i (gpu_ms: the whole batch's device time).
+ * Jobs of one geometry (same n, v, flags, and all static or all with their own seed), four or more of
+ * them, run as groups: one launch per pass for up to 2^24 bits of cyclic length, instead of one per pass
+ * and block (the reference's sub-block variant batches equal sub-blocks on cuFFT the same way,
+ * PrivacyAmplification_subblocks.cu:1058-1081); groups spread over the slots like single blocks.
+ * PA_BATCH_NO_GROUP launches every block on its own. */
 #define PA_BATCH_GRAPH 1u
 #define PA_BATCH_SERIAL 2u
 #define PA_BATCH_PERSISTENT 4u
+#define PA_BATCH_NO_GROUP 8u
 PA_API int pa_batch_run(pa_engine* e, const pa_job* jobs, uint32_t count, uint32_t batch_flags, void* stream);
+/* Group sizing: at least min_blocks (>= 2; 0 = 4) equal jobs form groups of up to 2^log_bits bits of
+ * cyclic length each (17..30; 0 = 24).  No batch may be pending. */
+PA_API int pa_set_groups(pa_engine* e, int32_t min_blocks, int32_t log_bits);
 PA_API int pa_batch_sync(pa_engine* e, pa_stats* stats, uint32_t count);
 
 /* PA_BATCH_PERSISTENT: the whole batch runs as ONE persistent kernel launch (with PA_BATCH_GRAPH, that

@@ -32,6 +32,7 @@ PA_PENDING = 1
 BATCH_GRAPH = 1
 BATCH_SERIAL = 2
 BATCH_PERSISTENT = 4
+BATCH_NO_GROUP = 8
 FLAG_XOR_KEY_REST = 1
 FLAG_COMPRESS = 2
 FLAG_EXACT = 4
@@ -43,7 +44,8 @@ EXPORTS = ("pa_create", "pa_destroy", "pa_set_seed", "pa_process", "pa_set_seed_
            "pa_stage_times", "pa_error_string", "pa_last_cuda_error", "pa_process_noalloc", "pa_set_pool",
            "pa_seed_cache_add", "pa_seed_cache_clear", "pa_batch_run", "pa_batch_sync", "pa_submit", "pa_poll",
            "pa_set_split", "pa_get_split", "pa_autotune", "pa_pool_reserve", "pa_selftest_wait_timeout",
-           "pa_set_lanes", "pa_serve_start", "pa_serve_submit", "pa_serve_poll", "pa_serve_stop")
+           "pa_set_lanes", "pa_serve_start", "pa_serve_submit", "pa_serve_poll", "pa_serve_stop", "pa_dft16_stages",
+           "pa_set_groups")
 
 
 class PAError(RuntimeError):
@@ -123,11 +125,14 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pa_autotune": ([eng, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
         "pa_pool_reserve": ([eng, ctypes.c_uint32, ctypes.c_int32], ctypes.c_int),
         "pa_set_lanes": ([eng, ctypes.c_int32, ctypes.c_uint32], ctypes.c_int),
+        "pa_set_groups": ([eng, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
         "pa_serve_start": ([eng, ctypes.c_int32, ctypes.c_uint32, ctypes.c_int32], ctypes.c_int),
         "pa_serve_submit": ([eng, ctypes.POINTER(PAJob), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
         "pa_serve_poll": ([eng, ctypes.c_uint64, ctypes.POINTER(PAStats)], ctypes.c_int),
         "pa_serve_stop": ([eng], ctypes.c_int),
         "pa_selftest_wait_timeout": ([ctypes.c_int32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+        "pa_dft16_stages": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32,
+                             ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -157,6 +162,19 @@ def process_noalloc(d_seed: int, d_key_start: int, d_key_rest: int, n: int, v: i
                                            stream or None)
     if rc != 0:
         raise PAError(rc, "pa_process_noalloc")
+
+
+DFT16_FP32, DFT16_TC_SPLIT, DFT16_TC_TF32 = 0, 1, 2
+
+
+def dft16_stages(d_in: int, d_out: int, butterflies: int, reps: int, method: int, d_err: int,
+                 ctas_per_sm: int = 4, stream: int = 0):
+    """pa_dft16_stages: `reps` radix-16 DFT stages on device data by FP32 butterflies (DFT16_FP32) or on
+    the tensor cores (DFT16_TC_SPLIT, FP32-level accuracy; DFT16_TC_TF32, one TF32 product); queued on
+    `stream`, not synchronised."""
+    rc = load_library().pa_dft16_stages(d_in, d_out, butterflies, reps, method, ctas_per_sm, d_err, stream or None)
+    if rc != 0:
+        raise PAError(rc, "pa_dft16_stages")
 
 
 def selftest_wait_timeout(device_id: int = 0, rounds: int = 4096) -> int:
@@ -282,6 +300,11 @@ class Engine:
         if rc < 0:
             self._check(rc, "pa_pool_reserve")
         return rc
+
+    def set_groups(self, min_blocks: int = 0, log_bits: int = 0):
+        """Grouped launches of equal jobs: at least min_blocks per group (0 = 4), up to 2^log_bits bits of
+        cyclic length per group (0 = 24)."""
+        self._check(self._lib.pa_set_groups(self._h, min_blocks, log_bits), "pa_set_groups")
 
     def set_lanes(self, ctas_per_lane: int = 0, max_np: int = 0) -> int:
         """Persistent lanes (PA_BATCH_PERSISTENT): CTAs per lane and the largest cyclic length they hold;

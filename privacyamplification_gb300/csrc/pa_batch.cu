@@ -42,6 +42,36 @@ struct SeedEntry {
     bool live = false;
 };
 
+// Grouped launches (pa_group.cu): jobs of one geometry, at least min_group of them (pa_set_groups), run
+// as one launch per pass for up to 2^group_log_bits bits of cyclic length per group; larger blocks run
+// alone.  Groups of a geometry spread over the batch's slot streams like single blocks, so passes of
+// different groups overlap.
+constexpr uint32_t kMinGroup = 4;
+constexpr int kGroupLogBits = 24;  // measured best for 2^27-bit banks of 2^18 .. 2^22-bit blocks
+
+// A group's working set: Y, Z and the group's own seed spectra (complex values each), bit rows / planes.
+struct GroupBuf {
+    float2* work = nullptr;
+    float2* work2 = nullptr;
+    float2* spec = nullptr;
+    uint32_t* planes = nullptr;
+    size_t work_cap = 0, planes_cap = 0, bytes = 0;
+};
+
+// One group of a batch: `count` jobs of geometry g, their entries from entry_off of the batch's table,
+// its working set the pool's group buffer of the same index.
+struct GroupChunk {
+    BlockGeom g{};
+    uint32_t flags = 0;
+    bool dynamic = false;  // every job brings its own seed
+    uint32_t count = 0;
+    size_t entry_off = 0;
+    double cost = 0.0;
+    pa::PassMaps maps{};
+};
+
+size_t group_planes_stride(const BlockGeom& g) { return (size_t(1) << g.log_np) / 32 + 64; }
+
 }  // namespace
 
 struct Slot {
@@ -140,10 +170,19 @@ struct Pool {
     uint32_t job_cap = 0;
     std::vector<pa_job> jobs;
     std::vector<BlockGeom> geoms;
-    std::vector<int> job_slot;
     cudaStream_t batch_stream = nullptr;
     bool batch_pending = false;
     std::unordered_map<uint64_t, cudaGraphExec_t> graphs;
+    // grouped launches: working sets, the pending batch's groups and their entry table (a captured
+    // graph keeps a table of its own, freed with it)
+    std::vector<GroupBuf> gbufs;
+    std::vector<GroupChunk> chunks;
+    std::vector<pa::GroupEntry> hentries;
+    pa::GroupEntry* gentries = nullptr;
+    size_t gentries_cap = 0;
+    std::unordered_map<uint64_t, pa::GroupEntry*> graph_entries;
+    uint32_t min_group = kMinGroup;
+    int group_log_bits = kGroupLogBits;
     // persistent lane launches
     LaneSet* lanes = nullptr;
     int lane_ctas = 4;        // CTAs per lane (pa_set_lanes)
@@ -248,7 +287,18 @@ void drop_lane_graphs(LaneSet* ls) {
 void drop_graphs(Pool* p) {
     for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second);
     p->graphs.clear();
+    for (auto& kv : p->graph_entries) cudaFree(kv.second);
+    p->graph_entries.clear();
     drop_lane_graphs(p->lanes);
+}
+
+void free_gbuf(Pool* p, GroupBuf& gb) {
+    cudaFree(gb.work);
+    cudaFree(gb.work2);
+    cudaFree(gb.spec);
+    cudaFree(gb.planes);
+    p->used -= std::min(p->used, gb.bytes);
+    gb = GroupBuf{};
 }
 
 void free_lanes(Pool* p) {
@@ -363,12 +413,26 @@ double job_cost(const BlockGeom& g, bool dynamic) {
     return np * g.log_np * (dynamic ? 1.6 : 1.0);
 }
 
-int batch_enqueue(pa_engine* e, Pool* p, const std::vector<std::vector<int>>& order, cudaStream_t s) {
+// order[k]: what slot k runs, a job index or -(group + 1); entries: the device copy of p->hentries.
+int batch_enqueue(pa_engine* e, Pool* p, const std::vector<std::vector<int>>& order, cudaStream_t s,
+                  const pa::GroupEntry* entries) {
     PA_CUDA(e, cudaEventRecord(p->fork, s));
     for (size_t k = 0; k < order.size(); ++k) {
         Slot* sl = p->slots[k];
         PA_CUDA(e, cudaStreamWaitEvent(sl->s, p->fork, 0));
         for (int j : order[k]) {
+            if (j < 0) {  // a group: one launch per pass for all its blocks
+                const GroupChunk& ch = p->chunks[(size_t)(-j - 1)];
+                const GroupBuf& gb = p->gbufs[(size_t)(-j - 1)];
+                const pa::Group gp{entries + ch.entry_off, ch.count, size_t(1) << ch.g.log_n,
+                                   group_planes_stride(ch.g)};
+                const pa::Scratch sc{gb.work, gb.work2, gb.planes, sl->err, &ch.maps};
+                int rc = pa::launch_group_prep(gp, sl->s);
+                if (!rc && ch.dynamic) rc = pa::launch_group_seed(ch.g, gp, gb.spec, sc, e->num_sms, sl->s);
+                if (!rc) rc = pa::launch_group_key(ch.g, gp, ch.flags, sc, e->num_sms, sl->s);
+                if (rc) return cuda_fail(e, (cudaError_t)rc);
+                continue;
+            }
             const pa_job& jb = p->jobs[j];
             const BlockGeom& g = p->geoms[j];
             unsigned long long* cnt = p->job_cnt + 2 * (size_t)j;
@@ -391,6 +455,106 @@ int batch_enqueue(pa_engine* e, Pool* p, const std::vector<std::vector<int>>& or
         }
         PA_CUDA(e, cudaEventRecord(sl->join, sl->s));
         PA_CUDA(e, cudaStreamWaitEvent(s, sl->join, 0));
+    }
+    return PA_OK;
+}
+
+// Groups of a batch: jobs of one geometry (three-pass; same n, v, flags and split; all static or all with
+// their own seed), p->min_group or more, cut into groups of at most 2^p->group_log_bits bits of cyclic
+// length (larger blocks run alone).  Fills p->chunks and p->hentries, sizes the group buffers (reallocating
+// one drops the captured graphs, which point into it) and marks the grouped jobs.  Groups nothing when
+// the buffers would not fit the HBM budget.
+int plan_groups(pa_engine* e, Pool* p, const pa_job* jobs, uint32_t count, const std::vector<BlockGeom>& geoms,
+                std::vector<char>& grouped) {
+    p->chunks.clear();
+    p->hentries.clear();
+    std::map<std::array<uint64_t, 4>, std::vector<int>> by;
+    for (uint32_t i = 0; i < count; ++i) {
+        const BlockGeom& g = geoms[i];
+        if (g.log_n1 == 0 || g.log_np >= p->group_log_bits) continue;
+        by[{((uint64_t)g.n << 32) | g.v, jobs[i].flags, (uint64_t)g.log_n2, jobs[i].seed_id < 0 ? 1ull : 0ull}]
+            .push_back((int)i);
+    }
+    for (auto& kv : by) {
+        const std::vector<int>& list = kv.second;
+        if (list.size() < p->min_group) continue;
+        const BlockGeom& g = geoms[list[0]];
+        const size_t per = size_t(1) << (p->group_log_bits - g.log_np);
+        for (size_t o = 0; o < list.size(); o += per) {
+            const size_t cnt = std::min(per, list.size() - o);
+            if (cnt < 2) break;  // a last single block runs alone
+            GroupChunk ch;
+            ch.g = g;
+            ch.flags = jobs[list[0]].flags;
+            ch.dynamic = jobs[list[0]].seed_id < 0;
+            ch.count = (uint32_t)cnt;
+            ch.entry_off = p->hentries.size();
+            for (size_t b = 0; b < cnt; ++b) {
+                const int j = list[o + b];
+                const pa_job& jb = jobs[j];
+                pa::GroupEntry en{};
+                en.key_start = jb.key_start;
+                en.key_rest = jb.key_rest;
+                en.out = reinterpret_cast<uint32_t*>(jb.out);
+                en.cnt = p->job_cnt + 2 * (size_t)j;
+                en.resid = p->job_resid + j;
+                if (ch.dynamic) {
+                    en.seed = jb.seed_words;  // spec: the group buffer's, below
+                } else {
+                    const SeedEntry& se = p->seeds[jb.seed_id];
+                    en.spec = se.spec;
+                    en.seed_cnt = se.cnt;
+                }
+                p->hentries.push_back(en);
+                ch.cost += job_cost(geoms[j], ch.dynamic);
+            }
+            p->chunks.push_back(ch);
+        }
+    }
+    // working sets: group c uses buffer c
+    size_t grow = 0;
+    for (size_t c = 0; c < p->chunks.size(); ++c) {
+        const GroupChunk& ch = p->chunks[c];
+        const size_t w = (size_t)ch.count << ch.g.log_n, pl = (size_t)ch.count * group_planes_stride(ch.g);
+        if (c >= p->gbufs.size() || p->gbufs[c].work_cap < w || p->gbufs[c].planes_cap < pl)
+            grow += 3 * w * sizeof(float2) + pl * 4;
+    }
+    if (p->used + grow > p->budget) {  // no room: every block runs alone
+        p->chunks.clear();
+        p->hentries.clear();
+        return PA_OK;
+    }
+    if (p->gbufs.size() < p->chunks.size()) p->gbufs.resize(p->chunks.size());
+    for (size_t c = 0; c < p->chunks.size(); ++c) {
+        GroupChunk& ch = p->chunks[c];
+        GroupBuf& gb = p->gbufs[c];
+        const size_t w = (size_t)ch.count << ch.g.log_n, pl = (size_t)ch.count * group_planes_stride(ch.g);
+        if (gb.work_cap < w || gb.planes_cap < pl) {
+            drop_graphs(p);
+            const size_t wc = std::max(w, gb.work_cap), pc = std::max(pl, gb.planes_cap);
+            free_gbuf(p, gb);
+            cudaError_t err = cudaMalloc(&gb.work, wc * sizeof(float2));
+            if (err == cudaSuccess) err = cudaMalloc(&gb.work2, wc * sizeof(float2));
+            if (err == cudaSuccess) err = cudaMalloc(&gb.spec, wc * sizeof(float2));
+            if (err == cudaSuccess) err = cudaMalloc(&gb.planes, pc * 4);
+            if (err != cudaSuccess) {
+                free_gbuf(p, gb);
+                return cuda_fail(e, err);
+            }
+            gb.work_cap = wc;
+            gb.planes_cap = pc;
+            gb.bytes = 3 * wc * sizeof(float2) + pc * 4;
+            p->used += gb.bytes;
+        }
+        if (ch.dynamic)
+            for (uint32_t b = 0; b < ch.count; ++b)
+                p->hentries[ch.entry_off + b].spec = gb.spec + ((size_t)b << ch.g.log_n);
+        int rc = pa::make_group_maps(ch.g, gb.work, gb.work2, ch.count, &ch.maps);
+        if (rc) return cuda_fail(e, (cudaError_t)rc);
+        for (uint32_t b = 0; b < ch.count; ++b) {
+            const pa::GroupEntry& en = p->hentries[ch.entry_off + b];
+            grouped[(size_t)(en.resid - p->job_resid)] = 1;
+        }
     }
     return PA_OK;
 }
@@ -768,6 +932,8 @@ void pool_destroy(pa_engine* e) {
     }
     cudaFree(p->job_cnt);
     cudaFree(p->job_resid);
+    for (GroupBuf& gb : p->gbufs) free_gbuf(p, gb);
+    cudaFree(p->gentries);
     if (p->fork) cudaEventDestroy(p->fork);
     if (p->b0) cudaEventDestroy(p->b0);
     if (p->b1) cudaEventDestroy(p->b1);
@@ -789,6 +955,18 @@ int pa_set_pool(pa_engine* e, uint64_t hbm_budget_bytes, int32_t max_slots, int3
     if (hbm_budget_bytes) p->budget = hbm_budget_bytes;
     p->max_slots = max_slots ? max_slots : 16;
     p->batch_slots = batch_slots ? batch_slots : 8;
+    drop_graphs(p);
+    return PA_OK;
+}
+
+int pa_set_groups(pa_engine* e, int32_t min_blocks, int32_t log_bits) {
+    if (!e || min_blocks < 0 || log_bits < 0 || (min_blocks && min_blocks < 2) || (log_bits && (log_bits < 17 || log_bits > 30)))
+        return PA_ERR_INVALID_ARG;
+    Pool* p = get_pool(e);
+    if (!p) return PA_ERR_CUDA;
+    if (p->batch_pending) return PA_ERR_BUSY;
+    p->min_group = min_blocks ? (uint32_t)min_blocks : kMinGroup;
+    p->group_log_bits = log_bits ? log_bits : kGroupLogBits;
     drop_graphs(p);
     return PA_OK;
 }
@@ -983,21 +1161,50 @@ int pa_batch_run(pa_engine* e, const pa_job* jobs, uint32_t count, uint32_t batc
         int rc = ensure_job_arrays(e, p, count);
         if (rc) return rc;
     }
-    // longest job first onto the least-loaded slot
-    std::vector<int> idx(count);
+    // groups of equal blocks, then every unit (a job alone or a group) longest first onto the
+    // least-loaded slot
+    std::vector<char> grouped(count, 0);
+    if (!(batch_flags & (PA_BATCH_SERIAL | PA_BATCH_NO_GROUP))) {
+        int rc = plan_groups(e, p, jobs, count, geoms, grouped);
+        if (rc) return rc;
+    } else {
+        p->chunks.clear();
+        p->hentries.clear();
+    }
+    std::vector<int> units;
+    std::vector<double> cost;
+    for (uint32_t i = 0; i < count; ++i)
+        if (!grouped[i]) {
+            units.push_back((int)i);
+            cost.push_back(job_cost(geoms[i], jobs[i].seed_id < 0));
+        }
+    for (size_t c = 0; c < p->chunks.size(); ++c) {
+        units.push_back(-(int)c - 1);
+        cost.push_back(p->chunks[c].cost);
+    }
+    std::vector<int> idx(units.size());
     std::iota(idx.begin(), idx.end(), 0);
-    std::vector<double> cost(count);
-    for (uint32_t i = 0; i < count; ++i) cost[i] = job_cost(geoms[i], jobs[i].seed_id < 0);
     if (!(batch_flags & PA_BATCH_SERIAL))
         std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
     std::vector<std::vector<int>> order(K);
     std::vector<double> load(K, 0.0);
-    p->job_slot.assign(count, 0);
-    for (int j : idx) {
+    for (int u : idx) {
         int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        order[k].push_back(j);
-        load[k] += cost[j];
-        p->job_slot[j] = k;
+        order[k].push_back(units[u]);
+        load[k] += cost[u];
+    }
+    // the groups' entry table (a pending batch finished before this one was accepted, so the table of a
+    // run without a graph is free to overwrite)
+    const size_t ne = p->hentries.size();
+    if (ne && !(batch_flags & PA_BATCH_GRAPH)) {
+        if (p->gentries_cap < ne) {
+            cudaFree(p->gentries);
+            p->gentries = nullptr;
+            p->gentries_cap = 0;
+            PA_CUDA(e, cudaMalloc(&p->gentries, ne * sizeof(pa::GroupEntry)));
+            p->gentries_cap = ne;
+        }
+        PA_CUDA(e, cudaMemcpy(p->gentries, p->hentries.data(), ne * sizeof(pa::GroupEntry), cudaMemcpyHostToDevice));
     }
     for (int k = 0; k < K; ++k) p->slots[k]->last_use = ++p->clock;
     PA_CUDA(e, cudaEventRecord(p->b0, s));
@@ -1008,25 +1215,43 @@ int pa_batch_run(pa_engine* e, const pa_job* jobs, uint32_t count, uint32_t batc
         for (const auto& g : geoms) key = fnv(key, &g, sizeof(g));
         auto it = p->graphs.find(key);
         if (it == p->graphs.end()) {
-            PA_CUDA(e, cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-            int rc = batch_enqueue(e, p, order, s);
-            cudaGraph_t graph = nullptr;
-            cudaError_t cerr = cudaStreamEndCapture(s, &graph);
-            if (rc) {
-                if (graph) cudaGraphDestroy(graph);
-                return rc;
+            if (p->graphs.size() >= 16) drop_graphs(p);
+            pa::GroupEntry* table = nullptr;  // the graph's own copy of the entries
+            if (ne) {
+                PA_CUDA(e, cudaMalloc(&table, ne * sizeof(pa::GroupEntry)));
+                cudaError_t cerr = cudaMemcpy(table, p->hentries.data(), ne * sizeof(pa::GroupEntry),
+                                              cudaMemcpyHostToDevice);
+                if (cerr != cudaSuccess) {
+                    cudaFree(table);
+                    return cuda_fail(e, cerr);
+                }
             }
-            if (cerr != cudaSuccess) return cuda_fail(e, cerr);
+            cudaError_t cerr = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+            if (cerr != cudaSuccess) {
+                cudaFree(table);
+                return cuda_fail(e, cerr);
+            }
+            int rc = batch_enqueue(e, p, order, s, table);
+            cudaGraph_t graph = nullptr;
+            cerr = cudaStreamEndCapture(s, &graph);
+            if (rc || cerr != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                cudaFree(table);
+                return rc ? rc : cuda_fail(e, cerr);
+            }
             cudaGraphExec_t exec = nullptr;
             cerr = cudaGraphInstantiate(&exec, graph, 0);
             cudaGraphDestroy(graph);
-            if (cerr != cudaSuccess) return cuda_fail(e, cerr);
-            if (p->graphs.size() >= 16) drop_graphs(p);
+            if (cerr != cudaSuccess) {
+                cudaFree(table);
+                return cuda_fail(e, cerr);
+            }
             it = p->graphs.emplace(key, exec).first;
+            if (table) p->graph_entries[key] = table;
         }
         PA_CUDA(e, cudaGraphLaunch(it->second, s));
     } else {
-        int rc = batch_enqueue(e, p, order, s);
+        int rc = batch_enqueue(e, p, order, s, p->gentries);
         if (rc) return rc;
     }
     PA_CUDA(e, cudaEventRecord(p->b1, s));

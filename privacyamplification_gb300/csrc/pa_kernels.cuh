@@ -69,23 +69,65 @@ int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32
 int kernel_count_key_block(const BlockGeom& g);   // kernels one key block launches
 int stage_count_key_block(const BlockGeom& g);    // timed stages (events - 1) of a key block
 
+// Grouped launches: G blocks of one geometry run as one launch per pass (grid dimension y, or z for the
+// two-dimensional transposes, is the block).  The group's working set is contiguous, block b's rows /
+// planes, Y, Z and own spectrum at base + b * stride; what the caller owns comes from a table of
+// entries in device memory.
+struct GroupEntry {
+    const uint32_t* key_start;
+    const uint32_t* key_rest;
+    const uint32_t* seed;                // the block's own seed words (a dynamic group), else null
+    const float2* spec;                  // the spectrum the key pass multiplies by
+    uint32_t* out;
+    unsigned long long* cnt;             // [0] key, [1] seed popcount
+    unsigned int* resid;                 // largest FP32 residual
+    const unsigned long long* seed_cnt;  // popcount of a cached seed (a static group), else null
+};
+struct Group {
+    const GroupEntry* e;  // null: one block, nothing offset
+    uint32_t count;       // blocks
+    size_t work;          // complex values per block in Y, Z and the group's own spectra
+    size_t planes;        // words per block of bit rows / parity planes
+};
+constexpr Group kOneBlock{nullptr, 1, 0, 0};
+// Zeroes each block's key popcount and residual word and copies a cached seed's popcount (or zero).
+int launch_group_prep(const Group& gp, cudaStream_t s);
+// The seed spectra of a dynamic group: block b's spectrum at spec + b * gp.work.
+int launch_group_seed(const BlockGeom& g, const Group& gp, float2* spec, const Scratch& sc, int num_sms,
+                      cudaStream_t s);
+// The key blocks of a group (after launch_group_prep and, for a dynamic group, launch_group_seed).
+int launch_group_key(const BlockGeom& g, const Group& gp, uint32_t flags, const Scratch& sc, int num_sms,
+                     cudaStream_t s);
+
 // Three-pass kernels (pa_passes.cu).  `rows` and the parity planes share one buffer of Np/8 bytes.
-int launch_bit_rows(const BlockGeom& g, const uint32_t* bits, bool seed, uint32_t* rows, cudaStream_t s);
+// With a group, the pointer arguments are the group's bases (rows, Y, Z, the own spectra) or are
+// replaced by the entries (bits, key_rest, out, cnt, resid, the key pass's spectrum).
+int launch_bit_rows(const BlockGeom& g, const uint32_t* bits, bool seed, uint32_t* rows, cudaStream_t s,
+                    const Group& gp = kOneBlock);
 int launch_pass_a(const BlockGeom& g, const uint32_t* rows, bool seed, float2* Y, unsigned long long* cnt,
-                  int num_sms, cudaStream_t s);
+                  int num_sms, cudaStream_t s, const Group& gp = kOneBlock);
 struct PassMaps {
     CUtensorMap y;  // Y (pass A output, row-major) as read by pass B
     CUtensorMap z;  // Z (pass B output, tile-major) as read by pass C
 };
 int make_pass_maps(const BlockGeom& g, const float2* Y, const float2* Z, PassMaps* out);
-// The Y and Z maps (out[0], out[1]) for columns of 2^log_n1, rows of 2^log_n2, pass B tiles of cpt columns.
-int encode_pass_maps(int log_n1, int log_n2, uint32_t cpt, const float2* Y, const float2* Z, CUtensorMap* out);
+// The maps of `blocks` consecutive blocks' Y and Z (a group's working set).
+int make_group_maps(const BlockGeom& g, const float2* Y, const float2* Z, uint32_t blocks, PassMaps* out);
+// The Y and Z maps (out[0], out[1]) for columns of 2^log_n1, rows of 2^log_n2, pass B tiles of cpt
+// columns, over `blocks` consecutive blocks.
+int encode_pass_maps(int log_n1, int log_n2, uint32_t cpt, const float2* Y, const float2* Z, CUtensorMap* out,
+                     uint32_t blocks = 1);
 int launch_pass_b(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y, float2* Z, float2* spec, int* err,
-                  int num_sms, cudaStream_t s);
+                  int num_sms, cudaStream_t s, const Group& gp = kOneBlock);
+// A group's pass B with columns of 2^LOGL (pa_group.cu), grid and shared memory as launch_pass_b chose.
+template <int LOGL>
+int launch_pass_b_group(bool seed, dim3 grid, size_t smem, const CUtensorMap& mapY, float2* Y, float2* Z,
+                        float2* spec, const BlockGeom& g, int* err, int early, const Group& gp, cudaStream_t s);
 int launch_pass_c(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
-                  uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s);
+                  uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s,
+                  const Group& gp = kOneBlock);
 int launch_finish(const BlockGeom& g, const uint32_t* planes, const uint32_t* key_rest, uint32_t flags,
-                  uint32_t* out, cudaStream_t s);
+                  uint32_t* out, cudaStream_t s, const Group& gp = kOneBlock);
 
 // Exact path (pa_ntt.cu): integer convolution modulo 3*2^30+1.  seed_hat, a, tmp: Np words each.
 struct NttTables;

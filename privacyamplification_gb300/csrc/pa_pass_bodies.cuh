@@ -270,8 +270,9 @@ struct PassBBases {
 // registers; every warp issues its share), or per-thread asynchronous copies when the tile is too wide
 // for a box.  Output (key pass): Z, tile-major (Z[tile][m1][CPT columns]), stored coalesced from
 // registers; (seed pass): spec.
-// The CTA takes tiles first, first + stride, ... (the kernel: blockIdx.x, gridDim.x).
-template <int LOGL, bool SEED, int NT>
+// The CTA takes tiles first, first + stride, ... (the kernel: blockIdx.x, gridDim.x).  GRP: blockIdx.y is
+// the block of a group, and mapY holds the group's blocks one after another, N1 rows each.
+template <int LOGL, bool SEED, int NT, bool GRP = false>
 __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const float2* __restrict__ Y,
                                              float2* __restrict__ Z, const BlockGeom& g, float2* __restrict__ spec,
                                              int* err, int early, uint32_t first, uint32_t stride) {
@@ -356,7 +357,8 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
         if ((t & 31) == 0) {
 #pragma unroll 1
             for (int b = b0 + (t >> 5); b < b1; b += NT / 32)
-                tma_load_2d(srow + b * BOXR * CPT, mapY, 2 * CPT * tl, BOXR * b, bb);
+                tma_load_2d(srow + b * BOXR * CPT, mapY, 2 * CPT * tl, (GRP ? (int)(blockIdx.y << g.log_n1) : 0) + BOXR * b,
+                            bb);
         }
     };
     auto load_tile = [&](int tl) {
@@ -679,7 +681,8 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
 // the last radix stage.  Their plane words keep whatever the buffer held: k_finish never reads a word
 // past out_bits.
 // BNT: threads of the pass B that wrote Z (its tile width is 32 BNT / N1 columns).  The CTA takes rows
-// first, first + stride, ... (the kernel: blockIdx.x, gridDim.x).
+// first, first + stride, ... (the kernel: blockIdx.x, gridDim.x).  blockIdx.y is the block of a group (0
+// otherwise): mapZ holds the group's blocks one after another, ntiles tiles each.
 template <int LOGL, int KEEP8, int BNT>
 __device__ __forceinline__ void pass_c_rows(const CUtensorMap* mapZ, const float2* __restrict__ Z, const BlockGeom& g,
                                             const unsigned long long* cnt, uint32_t* __restrict__ planes,
@@ -740,7 +743,7 @@ __device__ __forceinline__ void pass_c_rows(const CUtensorMap* mapZ, const float
         if (lane == 0) {
 #pragma unroll 1
             for (int b = b0 + (t >> 5); b < b1; b += NT / 32)
-                tma_load_3d(srow + (size_t)b * boxt * cpt, mapZ, 0, (int)r, boxt * b, bb);
+                tma_load_3d(srow + (size_t)b * boxt * cpt, mapZ, 0, (int)r, (int)blockIdx.y * ntiles + boxt * b, bb);
         }
     };
     auto load_early = [&](uint32_t r) {  // boxes [0, early) of row r (TMA only)

@@ -27,7 +27,11 @@ namespace pa {
 // 32c + 16h .. 32c + 16h + 15 -- one word of the row plane.
 template <bool SEED>
 __global__ void __launch_bounds__(256) k_bit_rows(const uint32_t* __restrict__ src, BlockGeom g,
-                                                  uint32_t* __restrict__ rows) {
+                                                  uint32_t* __restrict__ rows, Group gp) {
+    if (gp.e) {  // block blockIdx.z of a group
+        src = SEED ? gp.e[blockIdx.z].seed : gp.e[blockIdx.z].key_start;
+        rows += (size_t)blockIdx.z * gp.planes;
+    }
     const int lane = threadIdx.x & 31;
     const uint32_t n1 = 1u << g.log_n1, n2 = 1u << g.log_n2;
     const uint32_t a = blockIdx.x * 8u + (threadIdx.x >> 5);  // 16-row group
@@ -60,8 +64,12 @@ __global__ void __launch_bounds__(256) k_bit_rows(const uint32_t* __restrict__ s
 // transpose on distinct banks.  SEED: only for Np == n (the padded seed placement uses k_bit_rows).
 template <bool SEED>
 __global__ void __launch_bounds__(256) k_bit_rows_tiled(const uint32_t* __restrict__ src, BlockGeom g,
-                                                        uint32_t* __restrict__ rows) {
+                                                        uint32_t* __restrict__ rows, Group gp) {
     __shared__ uint32_t tile[256][17];  // [m2 - m20][a - a0], then [m1 - 16 a0][(m2 - m20) / 16]
+    if (gp.e) {
+        src = SEED ? gp.e[blockIdx.z].seed : gp.e[blockIdx.z].key_start;
+        rows += (size_t)blockIdx.z * gp.planes;
+    }
     const int t = threadIdx.x, lane = t & 31;
     const uint32_t win = (1u << g.log_n1) / 16u, wout = (1u << g.log_n2) / 16u;  // words per input / output row
     const uint32_t a0 = blockIdx.x * 16u, m20 = blockIdx.y * 256u;
@@ -104,12 +112,21 @@ __global__ void __launch_bounds__(256) k_bit_rows_tiled(const uint32_t* __restri
     }
 }
 
+// The pass kernels take block blockIdx.y of a group: its slices of the working set and its entry.
 template <int LOGL, bool SEED>
 __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
-    k_pass_a(const uint32_t* __restrict__ rows, BlockGeom g, float2* __restrict__ Y, unsigned long long* cnt) {
+    k_pass_a(const uint32_t* __restrict__ rows, BlockGeom g, float2* __restrict__ Y, unsigned long long* cnt,
+             Group gp) {
+    if (gp.e) {
+        rows += (size_t)blockIdx.y * gp.planes;
+        Y += (size_t)blockIdx.y * gp.work;
+        cnt = gp.e[blockIdx.y].cnt + (SEED ? 1 : 0);
+    }
     pass_a_rows<LOGL>(rows, g, Y, cnt, blockIdx.x, gridDim.x);
 }
 
+// One block (a group's pass B is k_pass_b_group in pa_group.cu: pass B runs at the 128-register limit
+// of two CTAs per SM, and this kernel keeps its pointers in the constant bank instead of registers).
 template <int LOGL, bool SEED>
 __global__ void __launch_bounds__(256, 2)
     k_pass_b(const __grid_constant__ CUtensorMap mapY, const float2* __restrict__ Y, float2* __restrict__ Z,
@@ -121,7 +138,13 @@ template <int LOGL, int KEEP8>
 __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
     k_pass_c(const __grid_constant__ CUtensorMap mapZ, const float2* __restrict__ Z, BlockGeom g,
              const unsigned long long* cnt, uint32_t* __restrict__ planes, unsigned int* resid_bits, int* err,
-             int early) {
+             int early, Group gp) {
+    if (gp.e) {  // (the body finds the block's tiles of mapZ from blockIdx.y)
+        Z += (size_t)blockIdx.y * gp.work;
+        cnt = gp.e[blockIdx.y].cnt;
+        planes += (size_t)blockIdx.y * gp.planes;
+        resid_bits = gp.e[blockIdx.y].resid;
+    }
     pass_c_rows<LOGL, KEEP8, 256>(&mapZ, Z, g, cnt, planes, resid_bits, err, early, blockIdx.x, gridDim.x);
 }
 
@@ -133,7 +156,12 @@ __global__ void __launch_bounds__((1 << LOGL) / 32, 1)
 // XORed with key_rest word ow.
 __global__ void __launch_bounds__(1024) k_finish(const uint32_t* __restrict__ planes, BlockGeom g,
                                                  const uint32_t* __restrict__ key_rest, uint32_t flags,
-                                                 uint32_t* __restrict__ out, uint32_t nwords) {
+                                                 uint32_t* __restrict__ out, uint32_t nwords, Group gp) {
+    if (gp.e) {  // block blockIdx.z of a group
+        planes += (size_t)blockIdx.z * gp.planes;
+        key_rest = gp.e[blockIdx.z].key_rest;
+        out = gp.e[blockIdx.z].out;
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t n1 = 1u << g.log_n1, wpr = (1u << g.log_n2) / 32u;
     const size_t plane_words = (size_t)n1 * wpr;
@@ -162,9 +190,14 @@ __global__ void __launch_bounds__(1024) k_finish(const uint32_t* __restrict__ pl
 // (64 bytes), with key_rest read the same way.
 __global__ void __launch_bounds__(256) k_finish_tiled(const uint32_t* __restrict__ planes, BlockGeom g,
                                                       const uint32_t* __restrict__ key_rest, uint32_t flags,
-                                                      uint32_t* __restrict__ out, uint32_t nwords) {
+                                                      uint32_t* __restrict__ out, uint32_t nwords, Group gp) {
     __shared__ uint32_t se[256][9], so[256][9];  // [m1 - m10][c - c0], even / odd samples
     __shared__ uint32_t sw[256][17];             // [m2 - 32 c0][(m1 - m10) / 16]
+    if (gp.e) {
+        planes += (size_t)blockIdx.z * gp.planes;
+        key_rest = gp.e[blockIdx.z].key_rest;
+        out = gp.e[blockIdx.z].out;
+    }
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const uint32_t n1 = 1u << g.log_n1, wpr = (1u << g.log_n2) / 32u;
     const size_t plane_words = (size_t)n1 * wpr;
@@ -222,39 +255,47 @@ static int grid_units(uint32_t units, int num_sms) {
     return (int)std::max<uint32_t>(1u, std::min<uint32_t>(units, (uint32_t)num_sms));
 }
 
-int launch_bit_rows(const BlockGeom& g, const uint32_t* bits, bool seed, uint32_t* rows, cudaStream_t s) {
+// CTAs per block of a (grouped) persistent pass: one wave of `per_wave` CTAs shared by the group's
+// blocks, at least one and at most `units` (rows or tiles) per block.  One block: min(units, per_wave).
+static int group_ctas(uint32_t units, int per_wave, const Group& gp) {
+    const uint32_t share = ((uint32_t)per_wave + gp.count - 1u) / gp.count;
+    return grid_units(units, (int)std::max<uint32_t>(1u, share));
+}
+
+int launch_bit_rows(const BlockGeom& g, const uint32_t* bits, bool seed, uint32_t* rows, cudaStream_t s,
+                    const Group& gp) {
     const uint32_t n1 = 1u << g.log_n1, n2 = 1u << g.log_n2;
     if (n1 >= 256u && n2 >= 256u && (!seed || (1u << g.log_np) == g.n)) {
-        dim3 grid(n1 / 256u, n2 / 256u);
-        if (seed) k_bit_rows_tiled<true><<<grid, 256, 0, s>>>(bits, g, rows);
-        else k_bit_rows_tiled<false><<<grid, 256, 0, s>>>(bits, g, rows);
+        dim3 grid(n1 / 256u, n2 / 256u, gp.count);
+        if (seed) k_bit_rows_tiled<true><<<grid, 256, 0, s>>>(bits, g, rows, gp);
+        else k_bit_rows_tiled<false><<<grid, 256, 0, s>>>(bits, g, rows, gp);
         return (int)cudaGetLastError();
     }
-    dim3 grid((n1 / 16u + 7u) / 8u, n2 / 32u);
-    if (seed) k_bit_rows<true><<<grid, 256, 0, s>>>(bits, g, rows);
-    else k_bit_rows<false><<<grid, 256, 0, s>>>(bits, g, rows);
+    dim3 grid((n1 / 16u + 7u) / 8u, n2 / 32u, gp.count);
+    if (seed) k_bit_rows<true><<<grid, 256, 0, s>>>(bits, g, rows, gp);
+    else k_bit_rows<false><<<grid, 256, 0, s>>>(bits, g, rows, gp);
     return (int)cudaGetLastError();
 }
 
 template <int LOGL>
 static int pass_a_l(const BlockGeom& g, const uint32_t* rows, bool seed, float2* Y, unsigned long long* cnt,
-                    int num_sms, cudaStream_t s) {
+                    int num_sms, cudaStream_t s, const Group& gp) {
     constexpr int NT = (1 << LOGL) / 32;
     size_t smem = (size_t)TileStride<(1 << LOGL)>::value * sizeof(float2);
-    int grid = grid_units(1u << g.log_n1, num_sms);
+    const dim3 grid(group_ctas(1u << g.log_n1, num_sms, gp), gp.count);
     if (seed) {
         smem_attr(k_pass_a<LOGL, true>, smem);
-        k_pass_a<LOGL, true><<<grid, NT, smem, s>>>(rows, g, Y, cnt);
+        k_pass_a<LOGL, true><<<grid, NT, smem, s>>>(rows, g, Y, cnt, gp);
     } else {
         smem_attr(k_pass_a<LOGL, false>, smem);
-        k_pass_a<LOGL, false><<<grid, NT, smem, s>>>(rows, g, Y, cnt);
+        k_pass_a<LOGL, false><<<grid, NT, smem, s>>>(rows, g, Y, cnt, gp);
     }
     return (int)cudaGetLastError();
 }
 
 template <int LOGL>
 static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y, float2* Z, float2* spec,
-                    int* err, int num_sms, cudaStream_t s) {
+                    int* err, int num_sms, cudaStream_t s, const Group& gp) {
     constexpr int L = 1 << LOGL, CPT = 8192 / L, RL = Plan<LOGL>::RA, NSL = L / RL;
     constexpr bool LEAN = LOGL <= 6;
     constexpr int U1N = LEAN ? 0 : (NSL < 16 ? NSL : 16), U2N = LEAN ? 0 : NSL / U1N;
@@ -262,7 +303,7 @@ static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2*
                              (size_t)PassBBases<LOGL, 256>::SLOTS * 256;
     static_assert(words * sizeof(float2) + 128 <= 112 * 1024, "pass B tile too large for two CTAs per SM");
     const size_t smem = words * sizeof(float2) + 128;  // + alignment of the TMA destination
-    int grid = grid_units((1u << g.log_n2) / CPT, 2 * num_sms);
+    const dim3 grid(group_ctas((1u << g.log_n2) / CPT, 2 * num_sms, gp), gp.count);
     // As many of the next tile's boxes as fit beside the tile while two CTAs stay resident per SM.
     constexpr int BOXR = L < 256 ? L : 256;
     const size_t box = (size_t)BOXR * CPT * sizeof(float2);
@@ -280,14 +321,15 @@ static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2*
         cudaGetLastError();  // a refused attribute above is not an error of this launch
         return e;
     };
+    static const int early_seed = early_boxes(k_pass_b<LOGL, true>);
+    static const int early_key = early_boxes(k_pass_b<LOGL, false>);
+    const int early = seed ? early_seed : early_key;
+    const size_t bytes = smem + (size_t)early * box;
+    if (gp.e) return launch_pass_b_group<LOGL>(seed, grid, bytes, maps.y, Y, Z, spec, g, err, early, gp, s);
     if (seed) {
-        static const int early = early_boxes(k_pass_b<LOGL, true>);
-        const size_t bytes = smem + (size_t)early * box;
         smem_attr(k_pass_b<LOGL, true>, bytes);
         k_pass_b<LOGL, true><<<grid, 256, bytes, s>>>(maps.y, Y, Z, g, spec, err, early);
     } else {
-        static const int early = early_boxes(k_pass_b<LOGL, false>);
-        const size_t bytes = smem + (size_t)early * box;
         smem_attr(k_pass_b<LOGL, false>, bytes);
         k_pass_b<LOGL, false><<<grid, 256, bytes, s>>>(maps.y, Y, Z, g, spec, err, early);
     }
@@ -320,7 +362,7 @@ static int pass_c_early(const BlockGeom& g, int logl, size_t exch_bytes, size_t 
 
 template <int LOGL, int KEEP8>
 static int pass_c_k(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
-                    uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s) {
+                    uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s, const Group& gp) {
     constexpr int NT = (1 << LOGL) / 32;
     const size_t exch = (size_t)TileStride<(1 << LOGL)>::value * sizeof(float2) + 128;  // + TMA alignment
     static const size_t static_bytes = [] {  // the kernel's own __shared__ arrays
@@ -333,8 +375,8 @@ static int pass_c_k(const BlockGeom& g, const PassMaps& maps, const float2* Z, c
     const size_t box_bytes = (size_t)(ntiles < 256u ? ntiles : 256u) * cpt * sizeof(float2);
     const size_t smem = exch + (size_t)early * box_bytes;
     smem_attr(k_pass_c<LOGL, KEEP8>, smem);
-    k_pass_c<LOGL, KEEP8><<<grid_units(1u << g.log_n1, num_sms), NT, smem, s>>>(maps.z, Z, g, cnt, planes, resid,
-                                                                               err, early);
+    const dim3 grid(group_ctas(1u << g.log_n1, num_sms, gp), gp.count);
+    k_pass_c<LOGL, KEEP8><<<grid, NT, smem, s>>>(maps.z, Z, g, cnt, planes, resid, err, early, gp);
     return (int)cudaGetLastError();
 }
 
@@ -351,14 +393,14 @@ static int pass_c_keep8(const BlockGeom& g, int rl) {
 // and every other ratio run the full last stage.
 template <int LOGL>
 static int pass_c_l(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
-                    uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s) {
+                    uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s, const Group& gp) {
     const int k8 = pass_c_keep8(g, Plan<LOGL>::RA);
     if constexpr (LOGL >= 12) {
-        if (k8 <= 2) return pass_c_k<LOGL, 2>(g, maps, Z, cnt, planes, resid, err, num_sms, s);
-        if (k8 == 3) return pass_c_k<LOGL, 3>(g, maps, Z, cnt, planes, resid, err, num_sms, s);
-        if (k8 == 4) return pass_c_k<LOGL, 4>(g, maps, Z, cnt, planes, resid, err, num_sms, s);
+        if (k8 <= 2) return pass_c_k<LOGL, 2>(g, maps, Z, cnt, planes, resid, err, num_sms, s, gp);
+        if (k8 == 3) return pass_c_k<LOGL, 3>(g, maps, Z, cnt, planes, resid, err, num_sms, s, gp);
+        if (k8 == 4) return pass_c_k<LOGL, 4>(g, maps, Z, cnt, planes, resid, err, num_sms, s, gp);
     }
-    return pass_c_k<LOGL, 8>(g, maps, Z, cnt, planes, resid, err, num_sms, s);
+    return pass_c_k<LOGL, 8>(g, maps, Z, cnt, planes, resid, err, num_sms, s, gp);
 }
 
 #define PA_ROWS_DISPATCH(LG, CALL)                   \
@@ -384,22 +426,22 @@ static int pass_c_l(const BlockGeom& g, const PassMaps& maps, const float2* Z, c
     }
 
 int launch_pass_a(const BlockGeom& g, const uint32_t* rows, bool seed, float2* Y, unsigned long long* cnt,
-                  int num_sms, cudaStream_t s) {
-#define C(LG) pass_a_l<LG>(g, rows, seed, Y, cnt, num_sms, s)
+                  int num_sms, cudaStream_t s, const Group& gp) {
+#define C(LG) pass_a_l<LG>(g, rows, seed, Y, cnt, num_sms, s, gp)
     PA_ROWS_DISPATCH(g.log_n2, C)
 #undef C
 }
 
 int launch_pass_b(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y, float2* Z, float2* spec, int* err,
-                  int num_sms, cudaStream_t s) {
-#define C(LG) pass_b_l<LG>(g, seed, maps, Y, Z, spec, err, num_sms, s)
+                  int num_sms, cudaStream_t s, const Group& gp) {
+#define C(LG) pass_b_l<LG>(g, seed, maps, Y, Z, spec, err, num_sms, s, gp)
     PA_COLS_DISPATCH(g.log_n1, C)
 #undef C
 }
 
 int launch_pass_c(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
-                  uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s) {
-#define C(LG) pass_c_l<LG>(g, maps, Z, cnt, planes, resid, err, num_sms, s)
+                  uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s, const Group& gp) {
+#define C(LG) pass_c_l<LG>(g, maps, Z, cnt, planes, resid, err, num_sms, s, gp)
     PA_ROWS_DISPATCH(g.log_n2, C)
 #undef C
 }
@@ -407,7 +449,8 @@ int launch_pass_c(const BlockGeom& g, const PassMaps& maps, const float2* Z, con
 // Tensor maps of the two strided transfers of a three-pass block with columns of 2^log_n1, rows of
 // 2^log_n2 and pass B tiles of cpt columns (see pass_b_tiles / pass_c_rows).  cuTensorMapEncodeTiled is
 // taken from the driver through the runtime, so the library does not link libcuda.
-int encode_pass_maps(int log_n1, int log_n2, uint32_t cpt, const float2* Y, const float2* Z, CUtensorMap* out) {
+int encode_pass_maps(int log_n1, int log_n2, uint32_t cpt, const float2* Y, const float2* Z, CUtensorMap* out,
+                     uint32_t blocks) {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         cudaDriverEntryPointQueryResult q;
@@ -420,8 +463,8 @@ int encode_pass_maps(int log_n1, int log_n2, uint32_t cpt, const float2* Y, cons
     }
     const uint64_t n1 = 1ull << log_n1, n2 = 1ull << log_n2;
     const cuuint32_t estr[3] = {1, 1, 1};
-    {   // Y: rows of 2 N2 floats; box = 2 cpt floats x min(N1, 256) rows
-        const cuuint64_t dims[2] = {2 * n2, n1};
+    {   // Y: rows of 2 N2 floats (N1 per block); box = 2 cpt floats x min(N1, 256) rows
+        const cuuint64_t dims[2] = {2 * n2, n1 * blocks};
         const cuuint64_t strides[1] = {2 * n2 * sizeof(float)};
         const cuuint32_t box[2] = {(cuuint32_t)(2 * cpt), (cuuint32_t)(n1 < 256 ? n1 : 256)};
         CUresult r = encode(&out[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(Y), dims, strides, box,
@@ -429,9 +472,9 @@ int encode_pass_maps(int log_n1, int log_n2, uint32_t cpt, const float2* Y, cons
                             CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return (int)cudaErrorInvalidValue;
     }
-    {   // Z: [tile][m1][2 cpt floats]; box = 2 cpt floats x 1 row x min(ntiles, 256) tiles
+    {   // Z: [tile][m1][2 cpt floats] (ntiles per block); box = 2 cpt floats x 1 row x min(ntiles, 256) tiles
         const uint64_t ntiles = n2 / cpt;
-        const cuuint64_t dims[3] = {2 * cpt, n1, ntiles};
+        const cuuint64_t dims[3] = {2 * cpt, n1, ntiles * blocks};
         const cuuint64_t strides[2] = {2 * cpt * sizeof(float), n1 * 2 * cpt * sizeof(float)};
         const cuuint32_t box[3] = {(cuuint32_t)(2 * cpt), 1, (cuuint32_t)(ntiles < 256 ? ntiles : 256)};
         CUresult r = encode(&out[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(Z), dims, strides, box,
@@ -444,12 +487,16 @@ int encode_pass_maps(int log_n1, int log_n2, uint32_t cpt, const float2* Y, cons
 
 // The per-pass kernels' maps (pass B with 256 threads: tiles of 8192 / N1 columns).
 int make_pass_maps(const BlockGeom& g, const float2* Y, const float2* Z, PassMaps* out) {
+    return make_group_maps(g, Y, Z, 1, out);
+}
+
+int make_group_maps(const BlockGeom& g, const float2* Y, const float2* Z, uint32_t blocks, PassMaps* out) {
     std::memset(out, 0, sizeof(*out));
     if (g.log_n1 == 0) return 0;
     const uint64_t cpt = 8192ull >> g.log_n1;
     if (cpt > 128) return 0;  // transfers use per-thread copies instead
     CUtensorMap m[2];
-    int rc = encode_pass_maps(g.log_n1, g.log_n2, (uint32_t)cpt, Y, Z, m);
+    int rc = encode_pass_maps(g.log_n1, g.log_n2, (uint32_t)cpt, Y, Z, m, blocks);
     if (rc) return rc;
     out->y = m[0];
     out->z = m[1];
@@ -457,19 +504,19 @@ int make_pass_maps(const BlockGeom& g, const float2* Y, const float2* Z, PassMap
 }
 
 int launch_finish(const BlockGeom& g, const uint32_t* planes, const uint32_t* key_rest, uint32_t flags,
-                  uint32_t* out, cudaStream_t s) {
+                  uint32_t* out, cudaStream_t s, const Group& gp) {
     const uint32_t n1 = 1u << g.log_n1, wpr = (1u << g.log_n2) / 32u;
     const uint32_t nwords = (g.out_bits + 31u) / 32u;
     // only plane columns that hold output samples: m2 < ceil(out_bits / (2 N1))
     const uint32_t m2max = (uint32_t)(((uint64_t)g.out_bits + 2ull * n1 - 1ull) / (2ull * n1));
     const uint32_t cols = std::min<uint32_t>(wpr, (m2max + 31u) / 32u);
     if (n1 >= 256u) {
-        dim3 grid(n1 / 256u, (cols + 7u) / 8u);
-        k_finish_tiled<<<grid, 256, 0, s>>>(planes, g, key_rest, flags, out, nwords);
+        dim3 grid(n1 / 256u, (cols + 7u) / 8u, gp.count);
+        k_finish_tiled<<<grid, 256, 0, s>>>(planes, g, key_rest, flags, out, nwords, gp);
         return (int)cudaGetLastError();
     }
-    dim3 grid((n1 / 32u + 3u) / 4u, (cols + 7u) / 8u);
-    k_finish<<<grid, 1024, 0, s>>>(planes, g, key_rest, flags, out, nwords);
+    dim3 grid((n1 / 32u + 3u) / 4u, (cols + 7u) / 8u, gp.count);
+    k_finish<<<grid, 1024, 0, s>>>(planes, g, key_rest, flags, out, nwords, gp);
     return (int)cudaGetLastError();
 }
 

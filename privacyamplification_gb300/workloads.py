@@ -12,6 +12,8 @@ hash bits.  Key material is drawn from fixed-seed PCG64 streams as i.i.d. Bernou
 * serve_device(): the same arrivals through the device-resident serving loop (pa_serve_*): the host
   only publishes request descriptors and reads completions; lanes on the GPU take requests as they free
   up, read the inputs from pinned host memory and write the outputs there.
+* sub_block_bank() + DeviceBank: equal sub-blocks of a 2^27-bit bank, the batched form of the reference's
+  sub-block variant, as one pa_batch_run.
 """
 from __future__ import annotations
 
@@ -24,6 +26,58 @@ import numpy as np
 from . import FLAG_COMPRESS, FLAG_XOR_KEY_REST, PAJob, output_bytes
 
 DEFAULT = FLAG_XOR_KEY_REST | FLAG_COMPRESS
+
+
+def random_block(n: int, v: int, rng_seed: int = 0x5EED):
+    """Seeded i.i.d. Bernoulli(0.5) seed and received-key words of one block (PCG64 stream `rng_seed`):
+    the synthetic inputs of every benchmark workload.  Returns (seed[n/32], recv_key[n/32+1])."""
+    rng = np.random.Generator(np.random.PCG64(rng_seed))
+    seed = rng.integers(0, 2 ** 32, size=n // 32, dtype=np.uint64).astype(np.uint32)
+    key = rng.integers(0, 2 ** 32, size=n // 32 + 1, dtype=np.uint64).astype(np.uint32)
+    return seed, key
+
+
+def sub_block_bank(log_s: int, bank_bits: int = 1 << 27, rng_seed: int = 0xBA4C):
+    """The sub-block bank of the reference's sub-block variant: bank_bits cut into B = bank_bits / s
+    blocks of s = 2^log_s bits with v = s/4 + s/8, each with its own seed and key (key2StartRest of its
+    own received key).  Returns (s, v, seeds[B, s/32], key_start[B, s/32], key_rest[B, v/32])."""
+    from . import key_split
+    s = 1 << log_s
+    v = s // 4 + s // 8
+    B = bank_bits // s
+    seeds = np.empty((B, s // 32), np.uint32)
+    ks = np.empty((B, s // 32), np.uint32)
+    kr = np.empty((B, v // 32), np.uint32)
+    for i in range(B):
+        seeds[i], recv = random_block(s, v, rng_seed + i)
+        ks[i], kr[i] = key_split(recv, s, v)
+    return s, v, seeds, ks, kr
+
+
+class DeviceBank:
+    """A sub-block bank on the device as pa_batch_run jobs: static seeds (one cached spectrum per block,
+    as the bank keeps one per sub-block) or each block's own seed."""
+
+    def __init__(self, engine, s, v, seeds, ks, kr, static: bool, device="cuda"):
+        import torch
+        self.engine, self.s, self.v, self.B = engine, s, v, seeds.shape[0]
+        dev = torch.device(device)
+        as_dev = lambda a: torch.from_numpy(np.ascontiguousarray(a).reshape(-1).view(np.int32)).to(dev)
+        self.d_seed, self.d_ks, self.d_kr = as_dev(seeds), as_dev(ks), as_dev(kr)
+        self.d_out = torch.zeros(self.B * (v // 8), dtype=torch.uint8, device=dev)
+        w, wr = s // 32, v // 32
+        sids = [engine.seed_cache_add(seeds[i], s, v, DEFAULT) for i in range(self.B)] if static else None
+        torch.cuda.synchronize()
+        self.jobs = [PAJob(None if static else self.d_seed.data_ptr() + 4 * w * i, sids[i] if static else -1,
+                           self.d_ks.data_ptr() + 4 * w * i, self.d_kr.data_ptr() + 4 * wr * i, s, v, DEFAULT,
+                           self.d_out.data_ptr() + (v // 8) * i) for i in range(self.B)]
+
+    def run(self, batch_flags=0, stream=0):
+        self.engine.batch_run(self.jobs, batch_flags, stream)
+        return self.engine.batch_sync(len(self.jobs))
+
+    def outputs(self):
+        return self.d_out.cpu().numpy().reshape(self.B, self.v // 8)
 
 
 @dataclass

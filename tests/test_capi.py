@@ -6,6 +6,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 import privacyamplification_gb300 as pa
 from oracle import oracle as O
@@ -17,7 +18,7 @@ HEADER = os.path.join(ROOT, "include", "pa_gb300.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(pa_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(pa_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_header_matches_binding_list():
@@ -73,3 +74,15 @@ def test_cufft_baseline_builds_and_exports():
     for name in ("cp_create", "cp_destroy", "cp_seed_slot", "cp_key_start_slot", "cp_key_rest_slot",
                  "cp_output_slot", "cp_process", "cp_residual"):
         assert hasattr(lib, name), name
+
+
+def test_dft16_stages_rejects_bad_arguments(pa_lib):
+    """Argument checks of the tensor-core stage measurement come before any CUDA call."""
+    import privacyamplification_gb300 as pa
+    bad = [(0, 0, 128, 1, pa.DFT16_FP32, 16), (16, 16, 100, 1, pa.DFT16_FP32, 16), (16, 16, 128, 0, 0, 16),
+           (16, 16, 128, 1, 3, 16), (16, 16, 128, 1, pa.DFT16_TC_SPLIT, 16, 5), (8, 16, 128, 1, 0, 16),
+           (16, 16, 128, 1, pa.DFT16_FP32, 16, 17)]
+    for a in bad:
+        with pytest.raises(pa.PAError) as e:
+            pa.dft16_stages(*a)
+        assert e.value.code == -1, a

@@ -133,3 +133,33 @@ def test_2p27_sha3_equal_to_reference_kernels(plain_lib, ref_kernels, gpu_engine
     finally:
         cp.use_restated_kernels()
         cp.close()
+
+
+@pytest.mark.parametrize("log_s,B", [(16, 8), (20, 2)])
+def test_sub_block_bank_matches_oracle_and_engine(plain_lib, log_s, B):
+    """The sub-block bank (B equal blocks on batched cuFFT plans) and the engine's batch of the same blocks
+    (static: one cached spectrum per block; dynamic: each block's own seed) against the oracle, block by
+    block, and against each other."""
+    from privacyamplification_gb300 import workloads as W
+    s, v, seeds, ks, kr = W.sub_block_bank(log_s, bank_bits=B << log_s, rng_seed=0x5B + log_s)
+    want = [(O.direct if s <= 1 << 16 else O.ntt)(seeds[i], ks[i], kr[i], s, v, DEFAULT) for i in range(B)]
+    bank = plain_lib.CufftBank(s, v, B)
+    try:
+        bank.load(seeds, ks, kr)
+        for recalc in (False, False, True):  # static: computed once, then reused; then recomputed
+            bank.run(recalc_seed=recalc)
+            got = bank.outputs()
+            for i in range(B):
+                assert np.array_equal(got[i], want[i]), (recalc, i)
+    finally:
+        bank.close()
+    with pa.Engine(max_sample_size=s) as eng:
+        for static in (True, False):
+            db = W.DeviceBank(eng, s, v, seeds, ks, kr, static)
+            for rep in range(2):
+                stats = db.run(pa.BATCH_GRAPH)
+                assert all(x.exact == 0 for x in stats)
+                mine = db.outputs()
+                for i in range(B):
+                    assert np.array_equal(mine[i], want[i]), (static, rep, i)
+            del db

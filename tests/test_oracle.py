@@ -107,3 +107,27 @@ def test_popcount():
     w = np.array([0xFFFFFFFF, 0x80000001, 0xF0000000], np.uint32)
     assert O.popcount(w, 96) == 32 + 2 + 4
     assert O.popcount(w, 34) == 33
+
+
+def test_workload_generator_matches_oracle_generator():
+    """The bench draws its inputs from the package's generator; the GPU tests rebuild them with the
+    oracle's: both must give the same words."""
+    from privacyamplification_gb300 import workloads as W
+    for n, v, sd in ((1 << 12, 1536, 7), (1 << 16, 24576, 0x5EED)):
+        a, b = W.random_block(n, v, sd), O.random_block(n, v, sd)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_sub_block_bank_layout(pa_lib):
+    """Sub-blocks of a bank: B = bank / s blocks with v = 3s/8, each key split by key2StartRest of its own
+    received key (bits past h of key_start are zero)."""
+    from privacyamplification_gb300 import workloads as W
+    s, v, seeds, ks, kr = W.sub_block_bank(12, bank_bits=6 << 12, rng_seed=3)
+    assert (s, v) == (4096, 1536) and seeds.shape == (6, 128) and ks.shape == (6, 128) and kr.shape == (6, 48)
+    h = s - v
+    for i in range(6):
+        seed, recv = O.random_block(s, v, 3 + i)
+        assert np.array_equal(seeds[i], seed)
+        k0, k1 = O.key_split(recv, s, v)
+        assert np.array_equal(ks[i], k0) and np.array_equal(kr[i], k1)
+        assert not ks[i][h // 32 + 1:].any()
