@@ -41,6 +41,16 @@ __host__ __device__ inline int seed_source(const BlockGeom& g, uint64_t x, uint6
     return 1;
 }
 
+// Source word of the placed seed's word x0 / 32 (x0 a multiple of 32).  n, v and so h, Np - h, Np - n and
+// seed_direct are multiples of 32 (the engine accepts no other sizes), so every boundary of the placement,
+// and every wrap of the filler and of the periodic form, falls between words: a placed word is one whole
+// source word, in the same MSB-first bit order.
+__host__ __device__ inline uint64_t seed_word(const BlockGeom& g, uint64_t x0) {
+    uint64_t s = 0;
+    seed_source(g, x0, &s);
+    return s >> 5;
+}
+
 }  // namespace pa
 
 // Host launch API (pa_kernels.cu).  All launches are asynchronous on `stream`.

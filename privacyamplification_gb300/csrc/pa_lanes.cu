@@ -84,12 +84,12 @@ __device__ __noinline__ void lane_bit_rows(const uint32_t* __restrict__ src, boo
                                               uint32_t stride) {
     const uint32_t n1 = 1u << g.log_n1, n2 = 1u << g.log_n2;
     // a power-of-two seed repeats with period n (word index mod n/32); any other n in a larger Np is placed
-    // bit by bit (seed_source)
+    // word by word (seed_word: the placement's boundaries fall between words)
     const bool periodic = seed && (g.n & (g.n - 1u)) == 0;
     const bool placed = seed && !periodic && (1u << g.log_np) != g.n;
     const uint64_t wmask = periodic ? (uint64_t)(g.n / 32u) - 1u : ~0ull;
     const int lane = threadIdx.x & 31;
-    if (n1 >= 256u && !placed) {
+    if (n1 >= 256u) {
         extern __shared__ __align__(16) uint32_t lane_smem[];
         uint32_t(*tile)[17] = reinterpret_cast<uint32_t(*)[17]>(lane_smem + (threadIdx.x >> 8) * (256 * 17));
         const int t = threadIdx.x & 255;
@@ -105,7 +105,8 @@ __device__ __noinline__ void lane_bit_rows(const uint32_t* __restrict__ src, boo
                 const int r = (t >> 4) + 16 * i, w = t & 15;
                 const uint64_t word = (uint64_t)(m20 + (uint32_t)r) * win + a0 + (uint32_t)w;
                 const uint64_t x0 = 32ull * word;
-                v[i] = (act && (seed || x0 <= g.h)) ? ld_in(src + (word & wmask), hostin) : 0u;
+                v[i] = (act && (seed || x0 <= g.h)) ? ld_in(src + (placed ? seed_word(g, x0) : (word & wmask)), hostin)
+                                                    : 0u;
             }
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
@@ -151,12 +152,7 @@ __device__ __noinline__ void lane_bit_rows(const uint32_t* __restrict__ src, boo
         } else if (!placed) {
             v = ld_in(src + ((x0 >> 5) & wmask), hostin);
         } else {
-            v = 0u;
-            for (int b = 0; b < 32; ++b) {
-                uint64_t s;
-                if (seed_source(g, x0 + b, &s)) v |= ((ld_in(src + (s >> 5), hostin) >> (31u - (uint32_t)(s & 31u))) & 1u)
-                                                     << (31 - b);
-            }
+            v = ld_in(src + seed_word(g, x0), hostin);
         }
         const uint32_t w = transpose16x2(v, lane);
         rows[(size_t)(16u * a + (uint32_t)(lane & 15)) * (n2 / 16u) + 2u * c + (uint32_t)(lane >> 4)] = w;

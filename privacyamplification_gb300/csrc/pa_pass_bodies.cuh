@@ -79,10 +79,6 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-__device__ __forceinline__ uint32_t load_bit(const uint32_t* __restrict__ w, uint64_t x) {
-    return (__ldg(w + (x >> 5)) >> (31u - (uint32_t)(x & 31u))) & 1u;
-}
-
 }  // namespace
 
 // ============================================================================ bit-plane transposes

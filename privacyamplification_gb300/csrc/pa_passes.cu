@@ -46,12 +46,8 @@ __global__ void __launch_bounds__(256) k_bit_rows(const uint32_t* __restrict__ s
         else v = __ldg(src + (x0 >> 5)) & ~(0xFFFFFFFFu >> (uint32_t)(g.h - x0 + 1));
     } else if ((1u << g.log_np) == g.n) {
         v = __ldg(src + (x0 >> 5));
-    } else {
-        v = 0u;
-        for (int b = 0; b < 32; ++b) {
-            uint64_t s;
-            if (seed_source(g, x0 + b, &s)) v |= load_bit(src, s) << (31 - b);
-        }
+    } else {  // padded placement: whole words
+        v = __ldg(src + seed_word(g, x0));
     }
     const uint32_t w = transpose16x2(v, lane);
     rows[(size_t)(16u * a + (uint32_t)(lane & 15)) * (n2 / 16u) + 2u * c + (uint32_t)(lane >> 4)] = w;
@@ -61,7 +57,7 @@ __global__ void __launch_bounds__(256) k_bit_rows(const uint32_t* __restrict__ s
 // input rows m2 (16 words of 16 m1 each, 64-byte segments) into shared memory, half-warp 16 x 16
 // transposes from there, and output rows m1 (16 words of 16 m2 each) back out -- every global access
 // is a 64-byte run instead of one word per row.  Rows padded to 17 words keep the column reads of the
-// transpose on distinct banks.  SEED: only for Np == n (the padded seed placement uses k_bit_rows).
+// transpose on distinct banks.  SEED with a padded Np: each word comes from its placed source word.
 template <bool SEED>
 __global__ void __launch_bounds__(256) k_bit_rows_tiled(const uint32_t* __restrict__ src, BlockGeom g,
                                                         uint32_t* __restrict__ rows, Group gp) {
@@ -80,7 +76,8 @@ __global__ void __launch_bounds__(256) k_bit_rows_tiled(const uint32_t* __restri
         const int r = (t >> 4) + 16 * i, w = t & 15;
         const uint64_t word = (uint64_t)(m20 + (uint32_t)r) * win + a0 + (uint32_t)w;
         const uint64_t x0 = 32ull * word;  // first sample of the word
-        v[i] = (SEED || x0 <= g.h) ? __ldg(src + word) : 0u;
+        if (SEED) v[i] = __ldg(src + ((1u << g.log_np) == g.n ? word : seed_word(g, x0)));
+        else v[i] = x0 <= g.h ? __ldg(src + word) : 0u;
     }
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
@@ -265,7 +262,7 @@ static int group_ctas(uint32_t units, int per_wave, const Group& gp) {
 int launch_bit_rows(const BlockGeom& g, const uint32_t* bits, bool seed, uint32_t* rows, cudaStream_t s,
                     const Group& gp) {
     const uint32_t n1 = 1u << g.log_n1, n2 = 1u << g.log_n2;
-    if (n1 >= 256u && n2 >= 256u && (!seed || (1u << g.log_np) == g.n)) {
+    if (n1 >= 256u && n2 >= 256u) {
         dim3 grid(n1 / 256u, n2 / 256u, gp.count);
         if (seed) k_bit_rows_tiled<true><<<grid, 256, 0, s>>>(bits, g, rows, gp);
         else k_bit_rows_tiled<false><<<grid, 256, 0, s>>>(bits, g, rows, gp);
