@@ -68,6 +68,7 @@ struct GroupChunk {
     size_t entry_off = 0;
     double cost = 0.0;
     pa::PassMaps maps{};
+    std::vector<int> jobs;  // job indices, in entry order
 };
 
 size_t group_planes_stride(const BlockGeom& g) { return (size_t(1) << g.log_np) / 32 + 64; }
@@ -506,6 +507,7 @@ int plan_groups(pa_engine* e, Pool* p, const pa_job* jobs, uint32_t count, const
                     en.seed_cnt = se.cnt;
                 }
                 p->hentries.push_back(en);
+                ch.jobs.push_back(j);
                 ch.cost += job_cost(geoms[j], ch.dynamic);
             }
             p->chunks.push_back(ch);
@@ -551,10 +553,7 @@ int plan_groups(pa_engine* e, Pool* p, const pa_job* jobs, uint32_t count, const
                 p->hentries[ch.entry_off + b].spec = gb.spec + ((size_t)b << ch.g.log_n);
         int rc = pa::make_group_maps(ch.g, gb.work, gb.work2, ch.count, &ch.maps);
         if (rc) return cuda_fail(e, (cudaError_t)rc);
-        for (uint32_t b = 0; b < ch.count; ++b) {
-            const pa::GroupEntry& en = p->hentries[ch.entry_off + b];
-            grouped[(size_t)(en.resid - p->job_resid)] = 1;
-        }
+        for (int j : ch.jobs) grouped[(size_t)j] = 1;
     }
     return PA_OK;
 }
