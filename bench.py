@@ -20,14 +20,16 @@ reference's definition (PrivacyAmplification.cu:1213, 2081).
 * roofline -- the dominant kernel's algorithmic bytes per launch / its mean CUDA-event duration in
             the timed region, against MEASURED_PEAKS.json's hbm_gbs.
 * cpu_baseline -- the exact NTT convolution of the oracle on all host cores, one whole block.
-* cufft_plain -- the reference's plain single-block GPU pipeline restated on cuFFT
-            (baseline/cufft_plain.cu: its kernels, launch shapes, pinned zero-copy slots and host syncs)
-            on the same GPU and inputs, static and dynamic seed, host wall time per block as the
-            reference's speedtest measures it; plus whether its output bytes equal the engine's.
-* --impl reference -- the reference has no CPU implementation of the path and its CUDA build cannot
-            run here (its sources are not on the GPU host), so this arm times the CPU port of the
-            GF(2) Toeplitz product (oracle, direct bit-packed rows) with all host threads on the same
-            workload: per step a row sample of a block, extrapolated to all v rows.
+* reference_cuda -- the reference's own kernels (compiled from PrivacyAmplification.cu for sm_103a by
+            baseline/ref_cuda.py) in its mainloop order on cuFFT, with its launch shapes, pinned
+            zero-copy slots and host syncs, on the same GPU and inputs, static and dynamic seed, host
+            wall time per block as the reference's speedtest measures it; plus whether its output
+            bytes equal the engine's.  cufft_plain: the same sequence with restated kernels.
+* other_configs -- short forms of configs 4 (the 512-block uneven mix as one CUDA graph) and 5 (2000
+            requests at 2000/s, host-driven serving); --workload batch / serve run them in full.
+* --impl reference -- the reference has no CPU implementation of the path, so this arm times the CPU
+            port (the oracle's exact NTT convolution, all host threads) on the same workload, one whole
+            block per step.
 
 For N > 1 (torchrun) every rank runs an independent replica on its own GPU (blocks are independent;
 no collective on the data path); value = all blocks of all ranks / max over ranks of the time.
@@ -568,11 +570,54 @@ def run_ours(args):
         "clocks": clk.summary(),
         "max_residual": stats.max_residual,
     }
-    print(json.dumps(line))
     eng.close()
+    if world == 1 and not args.no_configs:
+        line["other_configs"] = other_configs_leg(args)
+    print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def other_configs_leg(args):
+    """Short forms of configs 4 and 5 in the default run (their full forms are --workload batch / serve):
+    the 512-block uneven mix as one CUDA graph (device-timed, median of `steps` batches), and 2000
+    requests arriving at 2000/s with their own seeds (host-driven serving, p50 / p99)."""
+    import privacyamplification_gb300 as pa
+    from privacyamplification_gb300 import workloads as W
+    out = {}
+    with pa.Engine(max_sample_size=1 << 25) as eng:
+        eng.autotune(1 << 18, 1 << 26)
+        blocks = W.uneven_mix()
+        mix = W.DeviceMix(eng, blocks)
+        bits = sum(b.n for b in blocks)
+        for _ in range(args.warmup):
+            mix.run(pa.BATCH_GRAPH)
+        with ClockSampler(0) as clk:
+            ms = [mix.run(pa.BATCH_GRAPH)[0].gpu_ms for _ in range(max(3, min(args.steps, 10)))]
+        out["config4_batch"] = {
+            "workload": "512 blocks, n log-uniform [2^18, 2^25] (multiple of 1024), v/n ~ U[0.1,0.9], half with "
+                        "a cached static seed, half with their own; one CUDA graph per batch",
+            "gbit_s": bits / (statistics.median(ms) / 1e3) / 1e9, "ms_median": statistics.median(ms),
+            "ms_min": min(ms), "ms_max": max(ms), "batches": len(ms), "clocks": clk.summary()}
+    with pa.Engine(max_sample_size=1 << 27) as eng:
+        eng.pool_reserve(1 << 27, 16)
+        reqs = W.poisson_requests(2000, 2000, rng_seed=2000)
+        words = max(r.n // 32 + max(r.seed_word0, r.key_word0) for r in reqs) + 64
+        banks = W.HostBanks(words)
+        warm = W.poisson_requests(5000, 24, rng_seed=1)
+        for r in warm:
+            r.seed_word0 = r.key_word0 = 0
+        W.serve(eng, warm, banks)
+        with ClockSampler(0) as clk:
+            res = W.serve(eng, reqs, banks)
+        out["config5_serve_2000_per_s"] = {
+            "workload": "2000 requests, Poisson arrivals at 2000/s, n log-uniform [2^20, 2^27] (multiple of 1024), "
+                        "v/n ~ U[0.2,0.8], each with its own seed; host-driven pa_submit / pa_poll, 16 slots",
+            "p50_ms": res.pct(50), "p99_ms": res.pct(99), "sustained_gbit_s": res.bits / res.wall_s / 1e9,
+            "offered_gbit_s": sum(r.n for r in reqs) / reqs[-1].arrival / 1e9, "exact_recomputed": res.exact,
+            "clocks": clk.summary()}
+    return out
 
 
 # ------------------------------------------------------------------------------------ other workloads
@@ -898,6 +943,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-cufft", action="store_true", help="skip the cuFFT pipeline baseline leg")
+    ap.add_argument("--no-configs", action="store_true", help="skip the short config-4 / config-5 legs")
     ap.add_argument("--workload", default="static27",
                     choices=["static27", "dynamic27", "dynamic29", "exact29", "batch", "banked", "serve", "serve-static"],
                     help="static27 (default): the headline line; the others print their own line")
