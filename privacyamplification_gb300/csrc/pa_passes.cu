@@ -252,6 +252,18 @@ static int grid_units(uint32_t units, int num_sms) {
     return (int)std::max<uint32_t>(1u, std::min<uint32_t>(units, (uint32_t)num_sms));
 }
 
+// CTAs of `kernel` resident on one SM with `threads` threads and `smem` bytes of dynamic shared memory
+// (its dynamic shared-memory attribute already set); 1 if the query fails.
+template <class K>
+static int resident_ctas(K kernel, int threads, size_t smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        return 1;
+    }
+    return n;
+}
+
 // CTAs per block of a (grouped) persistent pass: one wave of `per_wave` CTAs shared by the group's
 // blocks, at least one and at most `units` (rows or tiles) per block.  One block: min(units, per_wave).
 static int group_ctas(uint32_t units, int per_wave, const Group& gp) {
@@ -279,14 +291,16 @@ static int pass_a_l(const BlockGeom& g, const uint32_t* rows, bool seed, float2*
                     int num_sms, cudaStream_t s, const Group& gp) {
     constexpr int NT = (1 << LOGL) / 32;
     size_t smem = (size_t)TileStride<(1 << LOGL)>::value * sizeof(float2);
-    const dim3 grid(group_ctas(1u << g.log_n1, num_sms, gp), gp.count);
-    if (seed) {
-        smem_attr(k_pass_a<LOGL, true>, smem);
-        k_pass_a<LOGL, true><<<grid, NT, smem, s>>>(rows, g, Y, cnt, gp);
-    } else {
-        smem_attr(k_pass_a<LOGL, false>, smem);
-        k_pass_a<LOGL, false><<<grid, NT, smem, s>>>(rows, g, Y, cnt, gp);
-    }
+    // a wave is every SM times the CTAs one SM holds: one for rows of 2^14, several for shorter rows
+    // (a row of 2^10 is one warp), so that short rows still fill the SMs
+    auto go = [&](auto kernel) {
+        smem_attr(kernel, smem);
+        static const int per_sm = resident_ctas(kernel, NT, smem);
+        const dim3 grid(group_ctas(1u << g.log_n1, num_sms * per_sm, gp), gp.count);
+        kernel<<<grid, NT, smem, s>>>(rows, g, Y, cnt, gp);
+    };
+    if (seed) go(k_pass_a<LOGL, true>);
+    else go(k_pass_a<LOGL, false>);
     return (int)cudaGetLastError();
 }
 
@@ -372,7 +386,8 @@ static int pass_c_k(const BlockGeom& g, const PassMaps& maps, const float2* Z, c
     const size_t box_bytes = (size_t)(ntiles < 256u ? ntiles : 256u) * cpt * sizeof(float2);
     const size_t smem = exch + (size_t)early * box_bytes;
     smem_attr(k_pass_c<LOGL, KEEP8>, smem);
-    const dim3 grid(group_ctas(1u << g.log_n1, num_sms, gp), gp.count);
+    const int per_sm = resident_ctas(k_pass_c<LOGL, KEEP8>, NT, smem);  // smem depends on the geometry
+    const dim3 grid(group_ctas(1u << g.log_n1, num_sms * per_sm, gp), gp.count);
     k_pass_c<LOGL, KEEP8><<<grid, NT, smem, s>>>(maps.z, Z, g, cnt, planes, resid, err, early, gp);
     return (int)cudaGetLastError();
 }
