@@ -13,16 +13,14 @@
 
 namespace pa {
 
-// A group's pass B: block blockIdx.y's slices of Y and Z, its spectrum (a seed pass writes the group's
-// own, a key pass reads the entry's), and its rows of mapY (the body reads blockIdx.y).
+// A group's pass B: the CTAs walk the tiles of all the group's blocks one after another (a seed pass
+// writes the group's own spectra, a key pass reads each entry's), so that a CTA's next tile -- often
+// another block's, short columns have few tiles -- is still copied under the current one.
 template <int LOGL, bool SEED>
 __global__ void __launch_bounds__(256, 2)
     k_pass_b_group(const __grid_constant__ CUtensorMap mapY, const float2* __restrict__ Y, float2* __restrict__ Z,
                    BlockGeom g, float2* __restrict__ spec, int* err, int early, Group gp) {
-    Y += (size_t)blockIdx.y * gp.work;
-    Z += (size_t)blockIdx.y * gp.work;
-    spec = SEED ? spec + (size_t)blockIdx.y * gp.work : const_cast<float2*>(gp.e[blockIdx.y].spec);
-    pass_b_tiles<LOGL, SEED, 256, true>(&mapY, Y, Z, g, spec, err, early, blockIdx.x, gridDim.x);
+    pass_b_tiles<LOGL, SEED, 256, true>(&mapY, Y, Z, g, spec, err, early, blockIdx.x, gridDim.x, gp.e, gp.count);
 }
 
 template <int LOGL>

@@ -266,12 +266,16 @@ struct PassBBases {
 // registers; every warp issues its share), or per-thread asynchronous copies when the tile is too wide
 // for a box.  Output (key pass): Z, tile-major (Z[tile][m1][CPT columns]), stored coalesced from
 // registers; (seed pass): spec.
-// The CTA takes tiles first, first + stride, ... (the kernel: blockIdx.x, gridDim.x).  GRP: blockIdx.y is
-// the block of a group, and mapY holds the group's blocks one after another, N1 rows each.
+// The CTA takes tiles first, first + stride, ... (the kernel: blockIdx.x, gridDim.x).  GRP: the tiles of
+// `nblocks` blocks of a group, one after another (unit u = block * ntiles + tile), so that a CTA's next
+// tile may be another block's and its copy still overlaps the current one; Y, Z, mapY and a seed pass's
+// spec hold the blocks one after another (N complex values, N1 rows of mapY each), and a key pass reads
+// block b's spectrum from ge[b].spec.
 template <int LOGL, bool SEED, int NT, bool GRP = false>
 __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const float2* __restrict__ Y,
                                              float2* __restrict__ Z, const BlockGeom& g, float2* __restrict__ spec,
-                                             int* err, int early, uint32_t first, uint32_t stride) {
+                                             int* err, int early, uint32_t first, uint32_t stride,
+                                             const GroupEntry* ge = nullptr, uint32_t nblocks = 1) {
     constexpr int L = 1 << LOGL, E = 32, CPT = 32 * NT / L, LR = L / 16, SP = TileStride<L>::value;
     constexpr bool TMA = CPT <= 128;              // box inner extent 2*CPT floats <= 256
     constexpr int BOXR = L < 256 ? L : 256;       // rows per box
@@ -310,6 +314,10 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
     __shared__ int s_fail;                      // a bounded wait expired: stop waiting
     const uint32_t n2 = 1u << g.log_n2;
     const int ntiles = (int)(n2 / CPT);
+    const int nunits = GRP ? ntiles * (int)nblocks : ntiles;
+    const int tshift = __ffs(ntiles) - 1;  // ntiles is a power of two
+    auto unit_tile = [&](int u) { return GRP ? (u & (ntiles - 1)) : u; };
+    auto unit_block = [&](int u) { return GRP ? (uint32_t)(u >> tshift) : 0u; };
     const int t = threadIdx.x;
     const int pp = t / LR, jj = t % LR;
     const float sc = 1.0f / (float)(4ull << g.log_np);  // seed spectrum scale 2X/(4Np)
@@ -347,26 +355,28 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
     // TMA boxes [b0, b1) of tile tl, called by every thread: thread 0 announces the bytes, lane 0 of
     // each warp issues every (NT/32)-th box (a copy landing first cannot complete the phase: its
     // arrival is pending).
-    auto load_boxes = [&](int tl, int b0, int b1, uint64_t* bb) {
-        if (tl >= ntiles || b0 >= b1) return;
+    auto load_boxes = [&](int u, int b0, int b1, uint64_t* bb) {
+        if (u >= nunits || b0 >= b1) return;
+        const int tl = unit_tile(u), y0 = (int)(unit_block(u) << g.log_n1);
         if (t == 0) mbar_expect_tx(bb, (uint32_t)((b1 - b0) * BOXR * CPT * sizeof(float2)));
         if ((t & 31) == 0) {
 #pragma unroll 1
             for (int b = b0 + (t >> 5); b < b1; b += NT / 32)
-                tma_load_2d(srow + b * BOXR * CPT, mapY, 2 * CPT * tl, (GRP ? (int)(blockIdx.y << g.log_n1) : 0) + BOXR * b,
-                            bb);
+                tma_load_2d(srow + b * BOXR * CPT, mapY, 2 * CPT * tl, y0 + BOXR * b, bb);
         }
     };
-    auto load_tile = [&](int tl) {
-        if (tl >= ntiles) return;
+    auto load_tile = [&](int u) {
+        if (u >= nunits) return;
         if (TMA) {
-            load_boxes(tl, 0, early, &bar_early);
-            load_boxes(tl, early, NBOX, &bar);
+            load_boxes(u, 0, early, &bar_early);
+            load_boxes(u, early, NBOX, &bar);
         } else {
+            const int tl = unit_tile(u);
+            const float2* Yb = Y + ((size_t)unit_block(u) << g.log_n);
 #pragma unroll 4
             for (int i = 0; i < L * CPT / 2 / NT; ++i) {
                 const int idx = t + i * NT, m1 = idx / (CPT / 2), cp = idx % (CPT / 2);
-                const float2* src = Y + (size_t)m1 * n2 + (size_t)tl * CPT + 2 * cp;
+                const float2* src = Yb + (size_t)m1 * n2 + (size_t)tl * CPT + 2 * cp;
                 cp_async8(sm + (2 * cp) * SP + padk<4>(m1), src);
                 cp_async8(sm + (2 * cp + 1) * SP + padk<4>(m1), src + 1);
             }
@@ -398,16 +408,20 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
     uint32_t parity_spec = 0;
     fence_proxy_async();
     load_tile((int)first);
-    for (int tile = (int)first; tile < ntiles; tile += (int)stride) {
+    for (int unit = (int)first; unit < nunits; unit += (int)stride) {
+        const int tile = unit_tile(unit);
+        const uint32_t blk = unit_block(unit);
+        // this block's spectrum: the seed pass writes it, the key pass reads it
+        float2* const bspec = !GRP ? spec : (SEED ? spec + ((size_t)blk << g.log_n) : const_cast<float2*>(ge[blk].spec));
         // the tile's seed spectrum (contiguous) is read after the forward FFT: start it into L2 now
         if (!SEED && t == 0)
-            prefetch_l2(spec + (size_t)tile * (CPT * L), CPT * L * sizeof(float2));
+            prefetch_l2(bspec + (size_t)tile * (CPT * L), CPT * L * sizeof(float2));
         if (!DIRECT || SEED) {
-            if (tile != (int)first) {
+            if (unit != (int)first) {
                 __syncthreads();  // previous tile done with sm
                 fence_proxy_async();
-                if (TMA) load_boxes(tile, early, NBOX, &bar);  // its first boxes came early
-                else load_tile(tile);
+                if (TMA) load_boxes(unit, early, NBOX, &bar);  // its first boxes came early
+                else load_tile(unit);
             }
         }
         wait_tile();
@@ -447,7 +461,7 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
         auto copy_early = [&]() {
             if (early > 0) {
                 fence_proxy_async();
-                load_boxes(tile + (int)stride, 0, early, &bar_early);
+                load_boxes(unit + (int)stride, 0, early, &bar_early);
             }
         };
         if (P::NSTAGE == 2) {
@@ -460,7 +474,7 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
         } else {
             exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorPair>(x, sm, copy_early);
         }
-        float2* tspec = spec + (size_t)tile * (CPT * L);
+        float2* tspec = bspec + (size_t)tile * (CPT * L);
         const bool special = tile == 0;  // pair 0 holds the self-mirrored columns 0 and N2/2
         // Key pass: the tile buffer is free until the inverse exchange, so the tile's seed spectrum
         // (CPT * L values, contiguous) is copied into it while the mirror stage computes, and the
@@ -613,8 +627,8 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
         if (DIRECT) {  // after the last exchange sm is free until the next tile: the rest of its boxes
             __syncthreads();
             fence_proxy_async();
-            if (TMA) load_boxes(tile + (int)stride, early, NBOX, &bar);
-            else load_tile(tile + (int)stride);
+            if (TMA) load_boxes(unit + (int)stride, early, NBOX, &bar);
+            else load_tile(unit + (int)stride);
         }
 #pragma unroll
         for (int q = 0; q < QL; ++q) {
@@ -634,7 +648,7 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
 #pragma unroll
             for (int r = 0; r < RL; ++r) x[q * RL + r] = cmul(x[q * RL + r], sigma[seq * RL + r]);
         }
-        float4* Z4 = reinterpret_cast<float4*>(Z) + (size_t)tile * L * (CPT / 2);  // this tile, [m1][CPT/2]
+        float4* Z4 = reinterpret_cast<float4*>(Z + ((size_t)blk << g.log_n)) + (size_t)tile * L * (CPT / 2);  // [m1][CPT/2]
         if (DIRECT) {  // thread holds column 0 (x[0..RL)) and column 1 (x[RL..2RL)) of rows j + NSL r
 #pragma unroll
             for (int r = 0; r < RL; ++r)

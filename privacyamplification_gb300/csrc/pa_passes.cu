@@ -314,7 +314,8 @@ static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2*
                              (size_t)PassBBases<LOGL, 256>::SLOTS * 256;
     static_assert(words * sizeof(float2) + 128 <= 112 * 1024, "pass B tile too large for two CTAs per SM");
     const size_t smem = words * sizeof(float2) + 128;  // + alignment of the TMA destination
-    const dim3 grid(group_ctas((1u << g.log_n2) / CPT, 2 * num_sms, gp), gp.count);
+    // a group's CTAs walk all its blocks' tiles (one dimension); one block's walk its own
+    const dim3 grid(grid_units(((1u << g.log_n2) / CPT) * gp.count, 2 * num_sms));
     // As many of the next tile's boxes as fit beside the tile while two CTAs stay resident per SM.
     constexpr int BOXR = L < 256 ? L : 256;
     const size_t box = (size_t)BOXR * CPT * sizeof(float2);
