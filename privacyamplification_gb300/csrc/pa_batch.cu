@@ -389,9 +389,22 @@ bool any_busy(Pool* p) {
     return false;
 }
 
-// Frees idle slots (least recently used first) until `need` more bytes fit the budget.
+// Frees the group working sets, then idle slots (least recently used first), until `need` more bytes
+// fit the budget.
 bool make_room(Pool* p, size_t need) {
     while (p->used + need > p->budget) {
+        if (!p->batch_pending) {  // group working sets first: only a pending batch uses them
+            bool freed = false;
+            for (GroupBuf& gb : p->gbufs)
+                if (gb.bytes) {
+                    free_gbuf(p, gb);
+                    freed = true;
+                }
+            if (freed) {
+                drop_graphs(p);
+                continue;
+            }
+        }
         Slot* victim = nullptr;
         for (Slot* sl : p->slots)
             if (!sl->busy && (!victim || sl->last_use < victim->last_use)) victim = sl;

@@ -165,3 +165,24 @@ def test_set_groups_arguments(pa_lib):
                 eng.set_groups(*a)
         eng.set_groups(2, 17)
         eng.set_groups(0, 0)
+
+
+def test_group_buffers_give_way_to_the_budget(torch_cuda):
+    """After a grouped batch, a tight HBM budget: adding a cached seed frees the group working sets
+    first; the next batch regroups if they fit again, or runs block by block, with the same outputs."""
+    n = 1 << 18
+    v = n // 4 + n // 8
+    with pa.Engine(max_sample_size=1 << 20) as eng:
+        bl = Blocks(torch_cuda, eng, n, v, 16, static=True, rng_seed=77)
+        want = [bl.want(i) for i in range(16)]
+        run(eng, bl.jobs, pa.BATCH_GRAPH)
+        eng.set_pool(64 << 20, 16, 8)  # below what the slots, spectra and group working set hold now
+        seed, _ = W.random_block(1 << 20, 1 << 18, 78)
+        eng.seed_cache_add(seed, 1 << 20, 1 << 18)
+        for flags in (0, pa.BATCH_GRAPH):
+            bl.d_out.fill_(0)
+            st = run(eng, bl.jobs, flags)
+            got = bl.outputs()
+            for i in range(16):
+                assert np.array_equal(got[i], want[i]), (flags, i)
+            assert all(s.exact == 0 for s in st)
