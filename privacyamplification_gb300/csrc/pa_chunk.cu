@@ -27,13 +27,14 @@ __global__ void k_seed_window(uint32_t* __restrict__ dst, const uint32_t* __rest
 }
 
 // Key chunk: sw words of key_start from bit `first` (a multiple of 32), bits past h cleared, then one
-// zero word (its first bit is the chunk's bit h' = s).
+// word whose first bit is the chunk's bit h' = s: zero, or with `extra` key bit first + s (= h, the one
+// tap past the last full column).
 __global__ void k_key_chunk(uint32_t* __restrict__ dst, const uint32_t* __restrict__ ks, unsigned long long first,
-                            uint32_t sw, uint32_t h) {
+                            uint32_t sw, uint32_t h, uint32_t extra) {
     for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w <= sw; w += gridDim.x * blockDim.x) {
         const unsigned long long bit = first + 32ull * w;
         uint32_t v = 0u;
-        if (w < sw && bit <= h) {
+        if ((w < sw || extra) && bit <= h) {
             v = __ldg(ks + (bit >> 5));
             if (bit + 31 > h) v &= ~(0xFFFFFFFFu >> (uint32_t)(h - bit + 1));
         }
@@ -75,6 +76,15 @@ ChunkPlan chunk_plan(const BlockGeom& g) {
     p.side = 1u << kChunkLog;
     p.rows = (g.out_bits + p.side - 1u) / p.side;
     p.cols = (uint32_t)(((uint64_t)g.h + 1u + p.side - 1u) / p.side);
+    // A chunk block's key has h' + 1 = side + 1 positions, the last one zero: when the taps past the last
+    // full column are exactly one (h = cols * side, e.g. v = 3n/8), that tap takes the last column's
+    // spare position instead of a column of its own.  Its seed index (i - h) lies in the column's seed
+    // window like every other tap's.
+    p.absorb = 0;
+    if (p.cols > 1 && ((uint64_t)g.h + 1u) % p.side == 1u) {
+        p.cols -= 1;
+        p.absorb = 1;
+    }
     p.chunks = p.rows * p.cols;
     p.diagonals = p.rows + p.cols - 1u;
     return p;
@@ -117,7 +127,8 @@ int launch_chunked_block(const BlockGeom& g, const BlockGeom& gc, const uint32_t
         if (rc) return rc;
         for (int a = a0; a < a1; ++a) {
             const int b = a - d;
-            k_key_chunk<<<gw, 256, 0, s>>>(keyc, key_start, (unsigned long long)b * p.side, sw, g.h);
+            const uint32_t extra = p.absorb && b == (int)p.cols - 1 ? 1u : 0u;
+            k_key_chunk<<<gw, 256, 0, s>>>(keyc, key_start, (unsigned long long)b * p.side, sw, g.h, extra);
             rc = launch_key_block(gc, keyc, nullptr, 0u, spec, sc, cnt, res + idx, cout, num_sms, s, nullptr);
             if (rc) return rc;
             k_xor_rows<<<gw, 256, 0, s>>>(acc + (size_t)a * sw, cout, sw);

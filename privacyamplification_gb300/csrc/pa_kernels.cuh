@@ -156,6 +156,7 @@ int exact_kernel_count(const BlockGeom& g);
 constexpr int kChunkLog = 26;
 struct ChunkPlan {
     uint32_t side, rows, cols, chunks, diagonals;
+    uint32_t absorb;  // 1: key bit h = cols * side (alone past the last full column) rides in that column
 };
 ChunkPlan chunk_plan(const BlockGeom& g);
 size_t chunk_staging_words(const BlockGeom& g);

@@ -121,10 +121,13 @@ def test_config3_2p29_dynamic_seed(big_engine):
 
 @pytest.mark.parametrize("n,v,flags", [(1 << 28, (1 << 26) + (1 << 25), DEFAULT),
                                        ((1 << 28) + (1 << 20), 100663296, pa.FLAG_COMPRESS),
-                                       ((1 << 28) - 1024, 33554432, pa.FLAG_XOR_KEY_REST)])
+                                       ((1 << 28) - 1024, 33554432, pa.FLAG_XOR_KEY_REST),
+                                       (1 << 28, 1 << 27, DEFAULT),
+                                       ((1 << 28) + (1 << 20), (1 << 27) + (1 << 20), pa.FLAG_COMPRESS)])
 def test_chunked_fp32_equals_exact_path(big_engine, n, v, flags):
     """Blocks beyond 2^27 bits: the FP32 chunk path reproduces the exact path bit for bit (whole
-    output), powers of two and not, with and without compression / XOR."""
+    output), powers of two and not, with and without compression / XOR.  The last two have h = 2^27,
+    a multiple of the chunk side: their one tap past the last full key column rides in that column."""
     seed, recv = O.random_block(n, v, n % 1000 + flags)
     ks, kr = pa.key_split(recv, n, v)
     big_engine.set_seed(seed, n, -1)
