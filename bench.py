@@ -781,7 +781,7 @@ def run_banked(args):
     pa.load_library()
     cufft_plain.build()
     sizes, total_bits, total_s = [], 0, 0.0
-    for log_s in (18, 20, 22, 25):
+    for log_s in (15, 18, 20, 22, 25):
         s, v, seeds, ks, kr = W.sub_block_bank(log_s)
         B = seeds.shape[0]
         bits = B * s
@@ -847,10 +847,10 @@ def run_banked(args):
         sizes.append(row)
     value = total_bits / total_s / 1e9
     _line(METRIC, value, UNIT, args.steps, args.warmup, total_s / len(sizes) * 1e3,
-          "sub-block banks: 2^27 bits as B equal blocks of s = 2^18 / 2^20 / 2^22 / 2^25 bits (B = 512 / 128 / 32 / "
-          "4), v = 3s/8, each block with its own seed and key; value: the engine's static-seed banks (one "
+          "sub-block banks: 2^27 bits as B equal blocks of s = 2^15 / 2^18 / 2^20 / 2^22 / 2^25 bits (B = 4096 / 512 / "
+          "128 / 32 / 4), v = 3s/8, each block with its own seed and key; value: the engine's static-seed banks (one "
           "CUDA graph of the bank's groups: one launch per pass for up to 2^27 bits of equal blocks) over all "
-          "four sizes",
+          "five sizes",
           {"sizes": sizes, "baseline": "the reference's sub-block variant (PrivacyAmplification_subblocks.cu) "
                                        "restated on batched cuFFT plans, device inputs, no host syncs "
                                        "(baseline/cufft_plain.cu cb_*)"})

@@ -473,8 +473,8 @@ int batch_enqueue(pa_engine* e, Pool* p, const std::vector<std::vector<int>>& or
     return PA_OK;
 }
 
-// Groups of a batch: jobs of one geometry (three-pass; same n, v, flags and split; all static or all with
-// their own seed), p->min_group or more, cut into groups of at most 2^p->group_log_bits bits of cyclic
+// Groups of a batch: jobs of one geometry (same n, v, flags and split; all static or all with their own
+// seed; single-CTA blocks too), p->min_group or more, cut into groups of at most 2^p->group_log_bits bits of cyclic
 // length (larger blocks run alone).  Fills p->chunks and p->hentries, sizes the group buffers (reallocating
 // one drops the captured graphs, which point into it) and marks the grouped jobs.  Groups nothing when
 // the buffers would not fit the HBM budget.
@@ -485,7 +485,7 @@ int plan_groups(pa_engine* e, Pool* p, const pa_job* jobs, uint32_t count, const
     std::map<std::array<uint64_t, 4>, std::vector<int>> by;
     for (uint32_t i = 0; i < count; ++i) {
         const BlockGeom& g = geoms[i];
-        if (g.log_n1 == 0 || g.log_np >= p->group_log_bits) continue;
+        if (g.log_np >= p->group_log_bits) continue;
         by[{((uint64_t)g.n << 32) | g.v, jobs[i].flags, (uint64_t)g.log_n2, jobs[i].seed_id < 0 ? 1ull : 0ull}]
             .push_back((int)i);
     }

@@ -66,7 +66,8 @@ int launch_group_prep(const Group& gp, cudaStream_t s) {
 
 int launch_group_seed(const BlockGeom& g, const Group& gp, float2* spec, const Scratch& sc, int num_sms,
                       cudaStream_t s) {
-    if (g.log_n1 == 0 || !gp.e) return (int)cudaErrorInvalidValue;
+    if (!gp.e) return (int)cudaErrorInvalidValue;
+    if (g.log_n1 == 0) return launch_group_mono_seed(g, gp, spec, s);
     int rc = launch_bit_rows(g, nullptr, true, sc.planes, s, gp);
     if (!rc) rc = launch_pass_a(g, sc.planes, true, sc.work, nullptr, num_sms, s, gp);
     if (!rc) rc = launch_pass_b(g, true, *sc.maps, sc.work, sc.work2, spec, sc.err, num_sms, s, gp);
@@ -75,7 +76,8 @@ int launch_group_seed(const BlockGeom& g, const Group& gp, float2* spec, const S
 
 int launch_group_key(const BlockGeom& g, const Group& gp, uint32_t flags, const Scratch& sc, int num_sms,
                      cudaStream_t s) {
-    if (g.log_n1 == 0 || !gp.e) return (int)cudaErrorInvalidValue;
+    if (!gp.e) return (int)cudaErrorInvalidValue;
+    if (g.log_n1 == 0) return launch_group_mono_key(g, gp, flags, s);
     int rc = launch_bit_rows(g, nullptr, false, sc.planes, s, gp);
     if (!rc) rc = launch_pass_a(g, sc.planes, false, sc.work, nullptr, num_sms, s, gp);
     if (!rc) rc = launch_pass_b(g, false, *sc.maps, sc.work, sc.work2, nullptr, sc.err, num_sms, s, gp);

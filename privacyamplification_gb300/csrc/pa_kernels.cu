@@ -123,11 +123,18 @@ __device__ __forceinline__ uint32_t mono_load(const uint32_t* __restrict__ bits,
     return ones;
 }
 
+// A group (gp.e set): block blockIdx.x of the group, its seed and popcount from its entry, its spectrum at
+// spec + blockIdx.x * gp.work.
 template <int N, int NT>
 __global__ void __launch_bounds__(NT) k_mono_seed(const uint32_t* __restrict__ seed, BlockGeom g,
-                                                  float2* __restrict__ spec, unsigned long long* cnt_seed) {
+                                                  float2* __restrict__ spec, unsigned long long* cnt_seed, Group gp) {
     extern __shared__ float2 sm[];
     __shared__ unsigned long long red[32];
+    if (gp.e) {
+        seed = gp.e[blockIdx.x].seed;
+        spec += (size_t)blockIdx.x * gp.work;
+        cnt_seed = gp.e[blockIdx.x].cnt + 1;
+    }
     uint32_t ones = mono_load<N, NT, true>(seed, g, sm);
     unsigned long long tot = block_sum(ones, red);
     if (threadIdx.x == 0) *cnt_seed = tot;
@@ -148,15 +155,25 @@ __global__ void __launch_bounds__(NT) k_mono_seed(const uint32_t* __restrict__ s
     }
 }
 
+// A group (gp.e set): block blockIdx.x of the group, everything it reads and writes from its entry.
 template <int N, int NT>
 __global__ void __launch_bounds__(NT) k_mono_key(const uint32_t* __restrict__ key_start,
                                                  const uint32_t* __restrict__ key_rest, BlockGeom g, uint32_t flags,
                                                  const float2* __restrict__ spec, unsigned long long* cnt,
-                                                 unsigned int* resid_bits, uint32_t* __restrict__ out_words) {
+                                                 unsigned int* resid_bits, uint32_t* __restrict__ out_words, Group gp) {
     extern __shared__ float2 sm[];
     __shared__ unsigned long long red[32];
     __shared__ float redf[32];
     __shared__ float s_corr;
+    if (gp.e) {
+        const GroupEntry& en = gp.e[blockIdx.x];
+        key_start = en.key_start;
+        key_rest = en.key_rest;
+        spec = en.spec;
+        cnt = en.cnt;
+        resid_bits = en.resid;
+        out_words = en.out;
+    }
     uint32_t ones = mono_load<N, NT, false>(key_start, g, sm);
     unsigned long long tot = block_sum(ones, red);
     if (threadIdx.x == 0) {
@@ -222,21 +239,22 @@ static constexpr int mono_threads() { return N >= 16384 ? 512 : (N / 16 < 32 ? 3
 
 template <int N>
 static int mono_seed(const BlockGeom& g, const uint32_t* seed, float2* spec, unsigned long long* cnt_seed,
-                     cudaStream_t s) {
+                     cudaStream_t s, const Group& gp = kOneBlock) {
     constexpr int NT = mono_threads<N>();
     size_t smem = (size_t)Padded<N>::value * sizeof(float2);
     set_smem(k_mono_seed<N, NT>, smem);
-    k_mono_seed<N, NT><<<1, NT, smem, s>>>(seed, g, spec, cnt_seed);
+    k_mono_seed<N, NT><<<gp.count, NT, smem, s>>>(seed, g, spec, cnt_seed, gp);
     return (int)cudaGetLastError();
 }
 
 template <int N>
 static int mono_key(const BlockGeom& g, const uint32_t* ks, const uint32_t* kr, uint32_t flags, const float2* spec,
-                    unsigned long long* cnt, unsigned int* resid, uint32_t* out, cudaStream_t s) {
+                    unsigned long long* cnt, unsigned int* resid, uint32_t* out, cudaStream_t s,
+                    const Group& gp = kOneBlock) {
     constexpr int NT = mono_threads<N>();
     size_t smem = (size_t)Padded<N>::value * sizeof(float2);
     set_smem(k_mono_key<N, NT>, smem);
-    k_mono_key<N, NT><<<1, NT, smem, s>>>(ks, kr, g, flags, spec, cnt, resid, out);
+    k_mono_key<N, NT><<<gp.count, NT, smem, s>>>(ks, kr, g, flags, spec, cnt, resid, out, gp);
     return (int)cudaGetLastError();
 }
 
@@ -295,6 +313,21 @@ int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32
     if (!rc) rc = launch_finish(g, sc.planes, key_rest, flags, out_words, s);
     mark(4);
     return rc;
+}
+
+// A group of single-CTA blocks: one CTA per block, one launch for the group.
+int launch_group_mono_seed(const BlockGeom& g, const Group& gp, float2* spec, cudaStream_t s) {
+    if (!gp.e) return (int)cudaErrorInvalidValue;
+#define C(NN) mono_seed<NN>(g, nullptr, spec, nullptr, s, gp)
+    PA_DISPATCH_MONO(g.log_n, C)
+#undef C
+}
+
+int launch_group_mono_key(const BlockGeom& g, const Group& gp, uint32_t flags, cudaStream_t s) {
+    if (!gp.e) return (int)cudaErrorInvalidValue;
+#define C(NN) mono_key<NN>(g, nullptr, nullptr, flags, nullptr, nullptr, nullptr, nullptr, s, gp)
+    PA_DISPATCH_MONO(g.log_n, C)
+#undef C
 }
 
 int kernel_count_key_block(const BlockGeom& g) { return g.log_n1 == 0 ? 1 : 5; }

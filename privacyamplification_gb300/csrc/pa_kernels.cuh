@@ -108,6 +108,9 @@ int launch_group_seed(const BlockGeom& g, const Group& gp, float2* spec, const S
 // The key blocks of a group (after launch_group_prep and, for a dynamic group, launch_group_seed).
 int launch_group_key(const BlockGeom& g, const Group& gp, uint32_t flags, const Scratch& sc, int num_sms,
                      cudaStream_t s);
+// The same for single-CTA geometries (n <= 2^15: one CTA per block; pa_kernels.cu).
+int launch_group_mono_seed(const BlockGeom& g, const Group& gp, float2* spec, cudaStream_t s);
+int launch_group_mono_key(const BlockGeom& g, const Group& gp, uint32_t flags, cudaStream_t s);
 
 // Three-pass kernels (pa_passes.cu).  `rows` and the parity planes share one buffer of Np/8 bytes.
 // With a group, the pointer arguments are the group's bases (rows, Y, Z, the own spectra) or are

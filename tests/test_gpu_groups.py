@@ -1,6 +1,7 @@
 """Grouped launches (pa_group.cu): equal blocks of a batch run as one launch per pass.  Every block's
 output is compared in full with the exact CPU oracle, and with the same batch launched block by block
-(PA_BATCH_NO_GROUP): static and own seeds, all flag combinations, a padded (non-power-of-two) geometry,
+(PA_BATCH_NO_GROUP): static and own seeds, single-CTA sizes (n <= 2^15) and three-pass ones, all flag
+combinations, padded (non-power-of-two) geometries,
 groups cut at 2^24 and 2^27 bits with a remainder, groups beside single blocks, graph capture and replay,
 and a block that trips the FP32 guard inside a group.
 """
@@ -68,7 +69,8 @@ def run(eng, jobs, flags):
     return eng.batch_sync(len(jobs))
 
 
-@pytest.mark.parametrize("log_n,count,static", [(18, 12, True), (18, 12, False), (20, 6, True), (16, 8, False)])
+@pytest.mark.parametrize("log_n,count,static", [(18, 12, True), (18, 12, False), (20, 6, True), (16, 8, False),
+                                               (12, 20, True), (15, 9, False), (10, 6, False)])
 def test_group_matches_oracle_and_single_launches(torch_cuda, log_n, count, static):
     n = 1 << log_n
     v = n // 4 + n // 8
@@ -95,6 +97,20 @@ def test_group_flag_variants(torch_cuda, flags):
         for i in range(5):
             assert np.array_equal(got[i], bl.want(i)), i
         assert all(s.exact == 0 for s in st)
+
+
+def test_group_padded_single_cta_geometry(torch_cuda):
+    """n = 3 * 2^10 (padded, one CTA per block): a group of single-CTA blocks, static and own seeds."""
+    n, v = 3 << 10, 1152
+    with pa.Engine(max_sample_size=1 << 13) as eng:
+        for static in (True, False):
+            bl = Blocks(torch_cuda, eng, n, v, 7, static=static, rng_seed=41)
+            for flags in (0, pa.BATCH_GRAPH):
+                bl.d_out.fill_(0x11)
+                run(eng, bl.jobs, flags)
+                got = bl.outputs()
+                for i in range(7):
+                    assert np.array_equal(got[i], bl.want(i)), (static, flags, i)
 
 
 def test_group_padded_geometry(torch_cuda):
