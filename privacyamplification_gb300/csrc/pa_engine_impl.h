@@ -89,7 +89,14 @@ inline int cuda_fail(pa_engine* e, cudaError_t err) {
 // rows 2^10..2^14 (passes A, C) and columns 2^5..2^12 (pass B).
 inline int split_min(int log_n) { return log_n - 12 > 10 ? log_n - 12 : 10; }
 inline int split_max(int log_n) { return log_n - 5 < 14 ? log_n - 5 : 14; }
-inline int split_default(int log_n) { return split_max(log_n); }
+// Row length (log2) by default, from the autotuner's choices on GB300 one block after another: from
+// N = 2^20 complex on, the shortest rows allowed (columns of 2^12, the longest pass B takes; rows of 2^14
+// at N = 2^26); below that, rows of N / 64 (2^10 .. 2^13).
+inline int split_default(int log_n) {
+    if (log_n >= 20) return split_min(log_n);
+    const int l = log_n - 6;
+    return l < split_min(log_n) ? split_min(log_n) : (l > split_max(log_n) ? split_max(log_n) : l);
+}
 
 // Block geometry (sizes, padded cyclic length, three-pass split) for (n, v, flags); `split` is a
 // per-log_n table of row exponents (0 entries and a null table mean the default).
