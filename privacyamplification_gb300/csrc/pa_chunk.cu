@@ -46,11 +46,14 @@ __global__ void k_xor_rows(uint32_t* __restrict__ acc, const uint32_t* __restric
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < words; i += gridDim.x * blockDim.x) acc[i] ^= add[i];
 }
 
-// Output words (reference byte-stream order) = accumulated rows XOR key_rest (byte-swapped words).
+// Output words (reference byte-stream order) = accumulated rows (of both lanes, acc2 may be null) XOR
+// key_rest (byte-swapped words).
 __global__ void k_chunk_final(uint32_t* __restrict__ out, const uint32_t* __restrict__ acc,
-                              const uint32_t* __restrict__ key_rest, uint32_t words, uint32_t v, uint32_t flags) {
+                              const uint32_t* __restrict__ acc2, const uint32_t* __restrict__ key_rest, uint32_t words,
+                              uint32_t v, uint32_t flags) {
     for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x) {
         uint32_t x = acc[w];
+        if (acc2) x ^= acc2[w];
         if ((flags & kXorFlag) && 32ull * w < v) x ^= __byte_perm(__ldg(key_rest + w), 0, 0x0123);
         out[w] = x;
     }
@@ -96,6 +99,14 @@ size_t chunk_staging_words(const BlockGeom& g) {
     return 5 * sw + (size_t)p.rows * sw + p.chunks + 64;
 }
 
+// Second lane: seed window (2 sw), key chunk (2 sw), chunk output (sw), row accumulators (rows sw), its
+// popcounts (4 words).
+size_t chunk_lane_words(const BlockGeom& g) {
+    const ChunkPlan p = chunk_plan(g);
+    const size_t sw = p.side / 32u;
+    return 5 * sw + (size_t)p.rows * sw + 64;
+}
+
 int chunk_kernel_count(const BlockGeom& g, const BlockGeom& gc) {
     const ChunkPlan p = chunk_plan(g);
     // per diagonal: 2 window copies + seed spectrum (3); per chunk: key chunk, key block, xor; then 2
@@ -105,41 +116,71 @@ int chunk_kernel_count(const BlockGeom& g, const BlockGeom& gc) {
 int launch_chunked_block(const BlockGeom& g, const BlockGeom& gc, const uint32_t* seed, const uint32_t* key_start,
                          const uint32_t* key_rest, uint32_t flags, uint32_t* out_words, uint32_t* staging,
                          float2* spec, const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits,
-                         int num_sms, cudaStream_t s) {
+                         int num_sms, cudaStream_t s, const ChunkLane* lane2) {
     const ChunkPlan p = chunk_plan(g);
     const uint32_t sw = p.side / 32u, nw = g.n / 32u;
-    uint32_t* seedwin = staging;            // 2 sw words
-    uint32_t* keyc = staging + 2 * sw;      // sw + 1 words (2 sw reserved)
-    uint32_t* cout = staging + 4 * sw;      // sw words
-    uint32_t* acc = staging + 5 * sw;       // rows * sw words
-    unsigned int* res = reinterpret_cast<unsigned int*>(acc + (size_t)p.rows * sw);  // one per chunk
-    cudaError_t err = cudaMemsetAsync(acc, 0, (size_t)p.rows * sw * sizeof(uint32_t), s);
-    if (err != cudaSuccess) return (int)err;
+    // Per lane: seed window (2 sw words), key chunk (sw + 1 words, 2 sw reserved), chunk output (sw),
+    // row accumulators (rows * sw; each lane its own, combined at the end), popcounts.  The chunks'
+    // residual words (one per chunk) are lane 0's.
+    struct Lane {
+        uint32_t *seedwin, *keyc, *cout, *acc;
+        unsigned long long* cnt;
+        float2* spec;
+        const Scratch* sc;
+        cudaStream_t s;
+    } lanes[2];
+    lanes[0] = {staging, staging + 2 * sw, staging + 4 * sw, staging + 5 * sw, cnt, spec, &sc, s};
+    unsigned int* res = reinterpret_cast<unsigned int*>(staging + 5 * sw + (size_t)p.rows * sw);  // one per chunk
+    const int nlanes = lane2 ? 2 : 1;
+    if (lane2) {
+        uint32_t* st = lane2->staging;
+        lanes[1] = {st, st + 2 * sw, st + 4 * sw, st + 5 * sw,
+                    reinterpret_cast<unsigned long long*>(st + 5 * sw + (size_t)p.rows * sw), lane2->spec, &lane2->sc,
+                    lane2->s};
+    }
+    for (int l = 0; l < nlanes; ++l) {
+        cudaError_t err = cudaMemsetAsync(lanes[l].acc, 0, (size_t)p.rows * sw * sizeof(uint32_t), s);
+        if (err != cudaSuccess) return (int)err;
+    }
+    if (lane2) {  // the second lane starts once the inputs and both accumulators are ready
+        cudaError_t err = cudaEventRecord(lane2->fork, s);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(lane2->s, lane2->fork, 0);
+        if (err != cudaSuccess) return (int)err;
+    }
     const int gw = grid_for(sw, num_sms);
     uint32_t idx = 0;
+    int diag = 0;  // diagonals alternate between the lanes
     for (int d = -(int)(p.cols - 1); d < (int)p.rows; ++d) {
         const int a0 = d > 0 ? d : 0;
         const int a1 = (int)p.rows < (int)p.cols + d ? (int)p.rows : (int)p.cols + d;
         if (a0 >= a1) continue;
-        k_seed_window<<<gw, 256, 0, s>>>(seedwin, seed, nw, (long long)d * sw, sw);
-        k_seed_window<<<gw, 256, 0, s>>>(seedwin + sw, seed, nw, (long long)(d - 1) * sw, sw);
-        int rc = launch_seed_spectrum(gc, seedwin, spec, sc, cnt + 1, num_sms, s);
+        const Lane& L = lanes[diag++ % nlanes];
+        k_seed_window<<<gw, 256, 0, L.s>>>(L.seedwin, seed, nw, (long long)d * sw, sw);
+        k_seed_window<<<gw, 256, 0, L.s>>>(L.seedwin + sw, seed, nw, (long long)(d - 1) * sw, sw);
+        int rc = launch_seed_spectrum(gc, L.seedwin, L.spec, *L.sc, L.cnt + 1, num_sms, L.s);
         if (rc) return rc;
         for (int a = a0; a < a1; ++a) {
             const int b = a - d;
             const uint32_t extra = p.absorb && b == (int)p.cols - 1 ? 1u : 0u;
-            k_key_chunk<<<gw, 256, 0, s>>>(keyc, key_start, (unsigned long long)b * p.side, sw, g.h, extra);
-            rc = launch_key_block(gc, keyc, nullptr, 0u, spec, sc, cnt, res + idx, cout, num_sms, s, nullptr);
+            k_key_chunk<<<gw, 256, 0, L.s>>>(L.keyc, key_start, (unsigned long long)b * p.side, sw, g.h, extra);
+            rc = launch_key_block(gc, L.keyc, nullptr, 0u, L.spec, *L.sc, L.cnt, res + idx, L.cout, num_sms, L.s,
+                                  nullptr);
             if (rc) return rc;
-            k_xor_rows<<<gw, 256, 0, s>>>(acc + (size_t)a * sw, cout, sw);
+            k_xor_rows<<<gw, 256, 0, L.s>>>(L.acc + (size_t)a * sw, L.cout, sw);
             ++idx;
         }
     }
-    err = cudaMemsetAsync(resid_bits, 0, sizeof(unsigned int), s);
+    if (lane2) {
+        cudaError_t err = cudaEventRecord(lane2->join, lane2->s);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(s, lane2->join, 0);
+        if (err != cudaSuccess) return (int)err;
+    }
+    cudaError_t err = cudaMemsetAsync(resid_bits, 0, sizeof(unsigned int), s);
     if (err != cudaSuccess) return (int)err;
     k_max_words<<<1, 256, 0, s>>>(resid_bits, res, (int)idx);
     const uint32_t owords = (g.out_bits + 31u) / 32u;
-    k_chunk_final<<<grid_for(owords, num_sms), 256, 0, s>>>(out_words, acc, key_rest, owords, g.v, flags);
+    k_chunk_final<<<grid_for(owords, num_sms), 256, 0, s>>>(out_words, lanes[0].acc, lane2 ? lanes[1].acc : nullptr,
+                                                            key_rest, owords, g.v, flags);
     return (int)cudaGetLastError();
 }
 

@@ -115,19 +115,47 @@ int seed_common(pa_engine* e, uint32_t n, int32_t reuse, cudaStream_t s) {
 // n > 2^27: the block as 2^27-bit FP32 chunk blocks (pa_chunk.cu).  The exact seed transform's buffer
 // is the chunks' staging area and the chunk spectra go through d_spec, so both caches are invalidated.
 // Block popcounts are not formed on this path (read_stats reports 0).
+//
+// Two lanes take the diagonals in turn.  The second lane's three-pass buffers are the upper halves of
+// d_work / d_work2 (each holds Np / 2 >= 2^27 complex here, a chunk block needs 2^26); its staging, bit
+// planes and seed spectrum follow the first lane's staging in d_exact_seed (Np >= 2^28 words, the four
+// need under 2^28); its stream is `side`, free here because the block waited for key_rest's copy.
 int chunked_block(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const BlockGeom& g, uint32_t flags,
                   uint32_t* d_out, cudaStream_t s) {
     BlockGeom gc;
     const uint32_t side = 1u << pa::kChunkLog;
     int rc = make_geom(2u * side, side, 0u, e->split, &gc);
     if (rc) return rc;
-    if (pa::chunk_staging_words(g) > (size_t(1) << e->cap_log_np)) return PA_ERR_TOO_LARGE;
+    const size_t np = size_t(1) << e->cap_log_np;
+    if (pa::chunk_staging_words(g) > np) return PA_ERR_TOO_LARGE;
     rc = ensure_maps(e, gc);
     if (rc) return rc;
     e->exact_valid = false;
     e->spec_valid = false;
+    auto align64 = [](size_t w) { return (w + 63u) & ~size_t(63); };
+    const size_t nc = size_t(1) << gc.log_n;                               // complex per three-pass buffer
+    const size_t w0 = align64(pa::chunk_staging_words(g));                 // first lane's staging
+    const size_t w1 = align64(pa::chunk_lane_words(g));                    // second lane's staging
+    const size_t wp = align64((size_t(1) << gc.log_np) / 32u + 64u);       // bit planes: Np / 8 + 256 bytes
+    pa::ChunkLane lane{};
+    const pa::ChunkLane* lp = nullptr;
+    if (2 * nc <= np / 2 && w0 + w1 + wp + 2 * nc <= np) {
+        if (e->lane_maps_key != pa_host::maps_key(gc)) {
+            rc = pa::make_pass_maps(gc, e->d_work + nc, e->d_work2 + nc, &e->lane_maps);
+            if (rc) return cuda_fail(e, (cudaError_t)rc);
+            e->lane_maps_key = pa_host::maps_key(gc);
+        }
+        uint32_t* base = e->d_exact_seed;
+        lane.staging = base + w0;
+        lane.sc = {e->d_work + nc, e->d_work2 + nc, base + w0 + w1, e->d_err, &e->lane_maps};
+        lane.spec = reinterpret_cast<float2*>(base + w0 + w1 + wp);
+        lane.s = e->side;
+        lane.fork = e->lane_fork;
+        lane.join = e->lane_join;
+        lp = &lane;
+    }
     rc = pa::launch_chunked_block(g, gc, e->d_seed, d_ks, d_kr, flags, d_out, e->d_exact_seed, e->d_spec, scratch(e),
-                                  e->d_cnt, e->d_resid, e->num_sms, s);
+                                  e->d_cnt, e->d_resid, e->num_sms, s, lp);
     if (rc) return cuda_fail(e, (cudaError_t)rc);
     return PA_OK;
 }
@@ -287,6 +315,8 @@ int pa_create(const pa_config* cfg, pa_engine** out) {
     if ((err = cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking)) != cudaSuccess) return fail(err);
     if ((err = cudaEventCreateWithFlags(&e->kr_ready, cudaEventDisableTiming)) != cudaSuccess) return fail(err);
     if ((err = cudaEventCreateWithFlags(&e->main_ready, cudaEventDisableTiming)) != cudaSuccess) return fail(err);
+    if ((err = cudaEventCreateWithFlags(&e->lane_fork, cudaEventDisableTiming)) != cudaSuccess) return fail(err);
+    if ((err = cudaEventCreateWithFlags(&e->lane_join, cudaEventDisableTiming)) != cudaSuccess) return fail(err);
     size_t np = 1ull << e->cap_log_np;
     size_t words = np / 32 + 64;
     if ((err = cudaMalloc(&e->d_key_start, words * 4)) != cudaSuccess) return fail(err);
@@ -333,6 +363,8 @@ void pa_destroy(pa_engine* e) {
     if (e->ev1) cudaEventDestroy(e->ev1);
     if (e->kr_ready) cudaEventDestroy(e->kr_ready);
     if (e->main_ready) cudaEventDestroy(e->main_ready);
+    if (e->lane_fork) cudaEventDestroy(e->lane_fork);
+    if (e->lane_join) cudaEventDestroy(e->lane_join);
     if (e->side) cudaStreamDestroy(e->side);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;

@@ -43,6 +43,11 @@ struct pa_engine {
     pa::BlockGeom exact_geom{};
     pa::PassMaps maps{};        // tensor maps for the geometry maps_key
     int maps_key = -1;
+    // second lane of the chunk blocks (n > 2^27): tensor maps over the upper halves of d_work / d_work2,
+    // its stream is `side`, and the events it forks and joins on
+    pa::PassMaps lane_maps{};
+    int lane_maps_key = -1;
+    cudaEvent_t lane_fork = nullptr, lane_join = nullptr;
     uint32_t* d_planes = nullptr;
     unsigned long long* d_cnt = nullptr;  // [0] key popcount, [1] seed popcount
     unsigned int* d_resid = nullptr;

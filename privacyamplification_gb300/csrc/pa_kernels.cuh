@@ -164,8 +164,19 @@ struct ChunkPlan {
 ChunkPlan chunk_plan(const BlockGeom& g);
 size_t chunk_staging_words(const BlockGeom& g);
 int chunk_kernel_count(const BlockGeom& g, const BlockGeom& gc);
+// A second lane for the chunk blocks: its own staging (chunk_lane_words(g) words), seed spectrum and
+// three-pass buffers, and a stream; the diagonals alternate between the lanes, so one lane's short kernels
+// and kernel tails overlap the other's work.  fork / join: events the lanes synchronise with.
+struct ChunkLane {
+    uint32_t* staging;
+    float2* spec;
+    Scratch sc;
+    cudaStream_t s;
+    cudaEvent_t fork, join;
+};
+size_t chunk_lane_words(const BlockGeom& g);
 int launch_chunked_block(const BlockGeom& g, const BlockGeom& gc, const uint32_t* seed, const uint32_t* key_start,
                          const uint32_t* key_rest, uint32_t flags, uint32_t* out_words, uint32_t* staging,
                          float2* spec, const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits,
-                         int num_sms, cudaStream_t s);
+                         int num_sms, cudaStream_t s, const ChunkLane* lane2 = nullptr);
 }  // namespace pa
