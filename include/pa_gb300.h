@@ -81,8 +81,9 @@ PA_API void pa_destroy(pa_engine* e);
 
 /* Sets the Toeplitz seed (n/32 words) and computes its cached FP32 spectrum.  reuse_seed_amount
  * follows the reference: 0 = this block only, k > 0 = the next k blocks, -1 = forever
- * (PrivacyAmplification.cu:1786, 2099-2101).  Replaces binInt2float(seed) + cufftExecR2C(seed)
- * (PrivacyAmplification.cu:1831, 1903). */
+ * (PrivacyAmplification.cu:1786, 2099-2101).  A seed for one block only (0 or 1) of 2^21 bits and more
+ * is transformed inside that block's column pass instead (no spectrum is stored).  Replaces
+ * binInt2float(seed) + cufftExecR2C(seed) (PrivacyAmplification.cu:1831, 1903). */
 PA_API int pa_set_seed(pa_engine* e, const uint32_t* seed_words, uint32_t n, int32_t reuse_seed_amount);
 
 /* Processes one block synchronously (host buffers, pageable or pinned).  key_rest may be NULL when

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpa_gb300.so")
 SOURCES = ["pa_kernels.cu", "pa_passes.cu", "pa_lanes.cu", "pa_ntt.cu", "pa_chunk.cu", "pa_engine.cu", "pa_batch.cu",
-           "pa_noalloc.cu", "pa_selftest.cu", "pa_dft_tc.cu", "pa_group.cu"]
+           "pa_noalloc.cu", "pa_selftest.cu", "pa_dft_tc.cu", "pa_group.cu", "pa_fused.cu"]
 HOST_SOURCES = ["pa_sha3.cpp", "pa_config.cpp", "pa_zmtp.cpp", "pa_service.cpp"]  # plain C++, no CUDA
 SERVICE_MAIN = "pa_service_main.cpp"
 SERVICE = os.path.join(HERE, "pa_service")

@@ -96,6 +96,11 @@ int build_spectrum(pa_engine* e, const BlockGeom& g, cudaStream_t s) {
     return PA_OK;
 }
 
+// The seed serves the next block only and that block's column pass can transform it (the fused pass).
+bool fuse_seed(const pa_engine* e, const BlockGeom& g) {
+    return e->seed_left == 1 && e->d_park && pa::fused_geom(g);
+}
+
 int seed_common(pa_engine* e, uint32_t n, int32_t reuse, cudaStream_t s) {
     e->seed_valid = true;
     e->seed_n = n;
@@ -107,9 +112,27 @@ int seed_common(pa_engine* e, uint32_t n, int32_t reuse, cudaStream_t s) {
         int rc = make_geom(n, n / 2u, PA_FLAG_COMPRESS, e->split, &g);
         if (rc) return rc;
         if (g.exact_only) return PA_OK;  // chunk spectra are built per block, the exact transform on demand
+        if (fuse_seed(e, g)) return PA_OK;  // transformed inside the block's column pass
         return build_spectrum(e, g, s);
     }
     return PA_OK;
+}
+
+// A block whose seed serves it alone: the seed's row pass into d_spec, then the fused column pass.
+// d_spec then holds no spectrum.
+int fused_block(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const BlockGeom& g, uint32_t flags,
+                uint32_t* d_out, cudaStream_t s, cudaEvent_t* sev, cudaEvent_t kr_ready) {
+    int rc = ensure_maps(e, g);
+    if (rc) return rc;
+    if (e->seed_maps_key != pa_host::maps_key(g)) {
+        rc = pa::make_pass_maps(g, e->d_spec, e->d_work2, &e->seed_maps);
+        if (rc) return cuda_fail(e, (cudaError_t)rc);
+        e->seed_maps_key = pa_host::maps_key(g);
+    }
+    e->spec_valid = false;
+    rc = pa::launch_fused_block(g, e->d_seed, d_ks, d_kr, flags, e->d_spec, e->seed_maps, e->d_park, e->park_ctas,
+                                scratch(e), e->d_cnt, e->d_resid, d_out, e->num_sms, s, sev, kr_ready);
+    return rc ? cuda_fail(e, (cudaError_t)rc) : PA_OK;
 }
 
 // n > 2^27: the block as 2^27-bit FP32 chunk blocks (pa_chunk.cu).  The exact seed transform's buffer
@@ -201,7 +224,8 @@ int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const
         if (e->seed_left > 0) --e->seed_left;
         return PA_OK;
     }
-    if (!e->spec_valid || !same_seed_geom(e->spec_geom, g)) {
+    const bool fused = (!e->spec_valid || !same_seed_geom(e->spec_geom, g)) && fuse_seed(e, g);
+    if (!fused && (!e->spec_valid || !same_seed_geom(e->spec_geom, g))) {
         int rc = build_spectrum(e, g, s);
         if (rc) return rc;
     }
@@ -216,9 +240,14 @@ int block_common(pa_engine* e, const uint32_t* d_ks, const uint32_t* d_kr, const
         e->tev_next = (slot + 1) % e->tev.size();
         e->tev_count = std::min(e->tev_count + 1, e->tev.size());
     }
-    int rc = pa::launch_key_block(g, d_ks, d_kr, flags, e->d_spec, scratch(e), e->d_cnt, e->d_resid, d_out,
-                                  e->num_sms, s, sev, kr_ready);
-    if (rc) return cuda_fail(e, (cudaError_t)rc);
+    if (fused) {
+        int rc = fused_block(e, d_ks, d_kr, g, flags, d_out, s, sev, kr_ready);
+        if (rc) return rc;
+    } else {
+        int rc = pa::launch_key_block(g, d_ks, d_kr, flags, e->d_spec, scratch(e), e->d_cnt, e->d_resid, d_out,
+                                      e->num_sms, s, sev, kr_ready);
+        if (rc) return cuda_fail(e, (cudaError_t)rc);
+    }
     PA_CUDA(e, cudaEventRecord(e->ev1, s));
     if (e->seed_left > 0) --e->seed_left;
     return PA_OK;
@@ -333,6 +362,11 @@ int pa_create(const pa_config* cfg, pa_engine** out) {
     if ((err = cudaMalloc(&e->d_planes, np_fp32 / 8 + 256)) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_cnt, 2 * sizeof(unsigned long long))) != cudaSuccess) return fail(err);
     if ((err = cudaMalloc(&e->d_resid, sizeof(unsigned int))) != cudaSuccess) return fail(err);
+    if (e->cap_log_np >= 21) {  // blocks with columns of 2^10 and more: the fused column pass's park
+        // one spectrum tile per CTA: two CTAs per SM, at most one per tile of the largest block
+        e->park_ctas = std::min<uint32_t>(2u * (uint32_t)e->num_sms, (uint32_t)((np / 2) / 8192u));
+        if ((err = cudaMalloc(&e->d_park, e->park_ctas * pa::kParkBytes)) != cudaSuccess) return fail(err);
+    }
     cudaMemset(e->d_cnt, 0, 2 * sizeof(unsigned long long));
     cudaMemset(e->d_resid, 0, sizeof(unsigned int));
     *out = e;
@@ -357,6 +391,7 @@ void pa_destroy(pa_engine* e) {
     cudaFree(e->d_planes);
     cudaFree(e->d_cnt);
     cudaFree(e->d_resid);
+    cudaFree(e->d_park);
     for (auto& a : e->tev)
         for (auto ev : a) cudaEventDestroy(ev);
     if (e->ev0) cudaEventDestroy(e->ev0);

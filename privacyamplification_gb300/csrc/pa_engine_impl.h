@@ -48,6 +48,12 @@ struct pa_engine {
     pa::PassMaps lane_maps{};
     int lane_maps_key = -1;
     cudaEvent_t lane_fork = nullptr, lane_join = nullptr;
+    // a seed that serves one block is transformed inside that block's column pass: its row pass output
+    // goes to d_spec (tensor maps seed_maps), its spectrum tiles to park (park_ctas * kParkBytes)
+    pa::PassMaps seed_maps{};
+    int seed_maps_key = -1;
+    float2* d_park = nullptr;
+    uint32_t park_ctas = 0;
     uint32_t* d_planes = nullptr;
     unsigned long long* d_cnt = nullptr;  // [0] key popcount, [1] seed popcount
     unsigned int* d_resid = nullptr;

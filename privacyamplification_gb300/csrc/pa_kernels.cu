@@ -315,6 +315,32 @@ int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32
     return rc;
 }
 
+int launch_fused_block(const BlockGeom& g, const uint32_t* seed, const uint32_t* key_start, const uint32_t* key_rest,
+                       uint32_t flags, float2* seed_y, const PassMaps& seed_maps, float2* park, uint32_t park_ctas,
+                       const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits, uint32_t* out_words,
+                       int num_sms, cudaStream_t s, cudaEvent_t* ev, cudaEvent_t key_rest_ready) {
+    if (!fused_geom(g)) return (int)cudaErrorInvalidValue;
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecord(ev[i], s);
+    };
+    cudaMemsetAsync(resid_bits, 0, sizeof(unsigned int), s);
+    cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), s);  // key and seed popcounts
+    mark(0);
+    int rc = launch_bit_rows(g, seed, true, sc.planes, s);
+    if (!rc) rc = launch_pass_a(g, sc.planes, true, seed_y, cnt + 1, num_sms, s);
+    if (!rc) rc = launch_bit_rows(g, key_start, false, sc.planes, s);
+    if (!rc) rc = launch_pass_a(g, sc.planes, false, sc.work, cnt, num_sms, s);
+    mark(1);
+    if (!rc) rc = launch_pass_b_fused(g, seed_maps, *sc.maps, sc.work2, park, park_ctas, sc.err, num_sms, s);
+    mark(2);
+    if (!rc) rc = launch_pass_c(g, *sc.maps, sc.work2, cnt, sc.planes, resid_bits, sc.err, num_sms, s);
+    mark(3);
+    if (!rc && key_rest_ready) rc = (int)cudaStreamWaitEvent(s, key_rest_ready, 0);  // key_rest copied meanwhile
+    if (!rc) rc = launch_finish(g, sc.planes, key_rest, flags, out_words, s);
+    mark(4);
+    return rc;
+}
+
 // A group of single-CTA blocks: one CTA per block, one launch for the group.
 int launch_group_mono_seed(const BlockGeom& g, const Group& gp, float2* spec, cudaStream_t s) {
     if (!gp.e) return (int)cudaErrorInvalidValue;

@@ -76,6 +76,14 @@ int launch_key_block(const BlockGeom& g, const uint32_t* key_start, const uint32
                      const float2* spec, const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits,
                      uint32_t* out_words, int num_sms, cudaStream_t s, cudaEvent_t* stage_ev,
                      cudaEvent_t key_rest_ready = nullptr);
+// A key block whose seed serves it alone, the seed's column transform fused into the key's column pass
+// (fused_geom(g) only): seed_y (N complex values, where the spectrum would go) receives the seed's row
+// pass, seed_maps are over seed_y, park holds park_ctas * kParkBytes; cnt[0] / cnt[1] receive the key and
+// seed popcounts.  Otherwise as launch_key_block (the seed's bit rows and row pass time as stage 0).
+int launch_fused_block(const BlockGeom& g, const uint32_t* seed, const uint32_t* key_start, const uint32_t* key_rest,
+                       uint32_t flags, float2* seed_y, const PassMaps& seed_maps, float2* park, uint32_t park_ctas,
+                       const Scratch& sc, unsigned long long* cnt, unsigned int* resid_bits, uint32_t* out_words,
+                       int num_sms, cudaStream_t s, cudaEvent_t* stage_ev, cudaEvent_t key_rest_ready = nullptr);
 int kernel_count_key_block(const BlockGeom& g);   // kernels one key block launches
 int stage_count_key_block(const BlockGeom& g);    // timed stages (events - 1) of a key block
 
@@ -136,6 +144,16 @@ int launch_pass_b(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y
 template <int LOGL>
 int launch_pass_b_group(bool seed, dim3 grid, size_t smem, const CUtensorMap& mapY, float2* Y, float2* Z,
                         float2* spec, const BlockGeom& g, int* err, int early, const Group& gp, cudaStream_t s);
+// The fused column pass of a block whose seed serves it alone (pa_fused.cu): seed_maps.y over the seed's
+// row-pass output, maps.y over the key's; park: park_ctas * kParkBytes, one spectrum tile per CTA.
+constexpr size_t kParkBytes = 8192 * sizeof(float2);
+inline bool fused_geom(const BlockGeom& g) { return g.log_n1 >= 10 && g.log_n1 <= 12; }
+int launch_pass_b_fused(const BlockGeom& g, const PassMaps& seed_maps, const PassMaps& maps, float2* Z, float2* park,
+                        uint32_t park_ctas, int* err, int num_sms, cudaStream_t s);
+template <int LOGL>
+int launch_pass_b_fused_k(dim3 grid, size_t smem_base, size_t box, int max_early, const CUtensorMap& mapYs,
+                          const CUtensorMap& mapY, float2* Z, const BlockGeom& g, float2* park, int* err,
+                          cudaStream_t s);
 int launch_pass_c(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
                   uint32_t* planes, unsigned int* resid, int* err, int num_sms, cudaStream_t s,
                   const Group& gp = kOneBlock);

@@ -271,13 +271,18 @@ struct PassBBases {
 // tile may be another block's and its copy still overlaps the current one; Y, Z, mapY and a seed pass's
 // spec hold the blocks one after another (N complex values, N1 rows of mapY each), and a key pass reads
 // block b's spectrum from ge[b].spec.
-template <int LOGL, bool SEED, int NT, bool GRP = false>
+// FUSED: a seed used by this block only.  Every tile is taken twice, first from the seed's row pass output
+// (mapYs) as a seed pass, its spectrum tile parked in this CTA's CPT * L values of `spec` (written and read
+// back by the same CTA a tile later, so it stays in L2), then from the key's (mapY) as a key pass against it.
+template <int LOGL, bool SEED, int NT, bool GRP = false, bool FUSED = false>
 __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const float2* __restrict__ Y,
                                              float2* __restrict__ Z, const BlockGeom& g, float2* __restrict__ spec,
                                              int* err, int early, uint32_t first, uint32_t stride,
-                                             const GroupEntry* ge = nullptr, uint32_t nblocks = 1) {
+                                             const GroupEntry* ge = nullptr, uint32_t nblocks = 1,
+                                             const CUtensorMap* mapYs = nullptr) {
     constexpr int L = 1 << LOGL, E = 32, CPT = 32 * NT / L, LR = L / 16, SP = TileStride<L>::value;
     constexpr bool TMA = CPT <= 128;              // box inner extent 2*CPT floats <= 256
+    static_assert(!FUSED || (TMA && !GRP && !SEED), "the fused pass is a one-block key pass with TMA tiles");
     constexpr int BOXR = L < 256 ? L : 256;       // rows per box
     using P = Plan<LOGL>;
     using Lin = MapLinear<NT>;
@@ -355,21 +360,21 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
     // TMA boxes [b0, b1) of tile tl, called by every thread: thread 0 announces the bytes, lane 0 of
     // each warp issues every (NT/32)-th box (a copy landing first cannot complete the phase: its
     // arrival is pending).
-    auto load_boxes = [&](int u, int b0, int b1, uint64_t* bb) {
+    auto load_boxes = [&](int u, int b0, int b1, uint64_t* bb, const CUtensorMap* map) {
         if (u >= nunits || b0 >= b1) return;
         const int tl = unit_tile(u), y0 = (int)(unit_block(u) << g.log_n1);
         if (t == 0) mbar_expect_tx(bb, (uint32_t)((b1 - b0) * BOXR * CPT * sizeof(float2)));
         if ((t & 31) == 0) {
 #pragma unroll 1
             for (int b = b0 + (t >> 5); b < b1; b += NT / 32)
-                tma_load_2d(srow + b * BOXR * CPT, mapY, 2 * CPT * tl, y0 + BOXR * b, bb);
+                tma_load_2d(srow + b * BOXR * CPT, map, 2 * CPT * tl, y0 + BOXR * b, bb);
         }
     };
-    auto load_tile = [&](int u) {
+    auto load_tile = [&](int u, const CUtensorMap* map) {
         if (u >= nunits) return;
         if (TMA) {
-            load_boxes(u, 0, early, &bar_early);
-            load_boxes(u, early, NBOX, &bar);
+            load_boxes(u, 0, early, &bar_early, map);
+            load_boxes(u, early, NBOX, &bar, map);
         } else {
             const int tl = unit_tile(u);
             const float2* Yb = Y + ((size_t)unit_block(u) << g.log_n);
@@ -407,28 +412,39 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
     __syncthreads();
     uint32_t parity_spec = 0;
     fence_proxy_async();
-    load_tile((int)first);
+    load_tile((int)first, FUSED ? mapYs : mapY);
     for (int unit = (int)first; unit < nunits; unit += (int)stride) {
+#pragma unroll
+    for (int part = 0; part < (FUSED ? 2 : 1); ++part) {
+        // sd: this part is a seed pass (FUSED: part 0 the seed's tile, part 1 the key's)
+        const bool sd = FUSED ? part == 0 : SEED;
+        const CUtensorMap* const map_self = FUSED && sd ? mapYs : mapY;
+        // the part after this one: FUSED alternates seed and key tiles, otherwise the next tile (formed
+        // where it is used, so that nothing extra stays live across the transform)
+        auto next_u = [&]() { return FUSED && sd ? unit : unit + (int)stride; };
+        auto map_next = [&]() { return FUSED ? (sd ? mapY : mapYs) : mapY; };
         const int tile = unit_tile(unit);
         const uint32_t blk = unit_block(unit);
         // this block's spectrum: the seed pass writes it, the key pass reads it
         float2* const bspec = !GRP ? spec : (SEED ? spec + ((size_t)blk << g.log_n) : const_cast<float2*>(ge[blk].spec));
         // the tile's seed spectrum (contiguous) is read after the forward FFT: start it into L2 now
-        if (!SEED && t == 0)
+        if (!FUSED && !SEED && t == 0)
             prefetch_l2(bspec + (size_t)tile * (CPT * L), CPT * L * sizeof(float2));
-        if (!DIRECT || SEED) {
-            if (unit != (int)first) {
-                __syncthreads();  // previous tile done with sm
-                fence_proxy_async();
-                if (TMA) load_boxes(unit, early, NBOX, &bar);  // its first boxes came early
-                else load_tile(unit);
-            }
+        // The rest of a part's boxes were issued by the part before it when that was a DIRECT key pass
+        // (after its last exchange); otherwise here, once every thread is done with sm.
+        const bool preloaded = DIRECT && (FUSED ? sd : !SEED);
+        const bool first_part = unit == (int)first && (!FUSED || sd);
+        if (!preloaded && !first_part) {
+            __syncthreads();  // previous tile done with sm
+            fence_proxy_async();
+            if (TMA) load_boxes(unit, early, NBOX, &bar, map_self);  // its first boxes came early
+            else load_tile(unit, map_self);
         }
         wait_tile();
         __syncthreads();  // tile copies visible; previous tile done with the tables
         // The tile's column tables are first read by the last inverse stage, several block barriers
         // later: no barrier of their own, so the few threads computing them overlap the first stages.
-        if (!SEED) {
+        if (!sd) {
             for (int i = t; i < CPT * (RL + U1N + U2N); i += NT) {
                 int c, kind, r;
                 if (i < CPT * RL) { c = i / RL; r = i % RL; kind = 0; }
@@ -461,7 +477,7 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
         auto copy_early = [&]() {
             if (early > 0) {
                 fence_proxy_async();
-                load_boxes(unit + (int)stride, 0, early, &bar_early);
+                load_boxes(next_u(), 0, early, &bar_early, map_next());
             }
         };
         if (P::NSTAGE == 2) {
@@ -474,12 +490,12 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
         } else {
             exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorPair>(x, sm, copy_early);
         }
-        float2* tspec = bspec + (size_t)tile * (CPT * L);
+        float2* tspec = FUSED ? spec + (size_t)first * (CPT * L) : bspec + (size_t)tile * (CPT * L);
         const bool special = tile == 0;  // pair 0 holds the self-mirrored columns 0 and N2/2
         // Key pass: the tile buffer is free until the inverse exchange, so the tile's seed spectrum
         // (CPT * L values, contiguous) is copied into it while the mirror stage computes, and the
         // spectral step reads shared memory instead of waiting on L2.
-        const bool spec_smem = !SEED && !special;
+        const bool spec_smem = !sd && !special;
         if (spec_smem) {
             __syncthreads();  // every thread done reading sm
             fence_proxy_async();
@@ -536,7 +552,7 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
                     if (u == 0) {  // DC (dropped) and Nyquist in slot (0, 0); then the self pair N/2
                         float2 z = sm[padk<4>(0)];
                         float nyq = 2.0f * (z.x - z.y);
-                        if (SEED) {
+                        if (sd) {
                             tspec[spec_index<LR>(0, 0)] = make_float2(nyq * sc, 0.f);
                         } else {
                             float pn = nyq * tspec[spec_index<LR>(0, 0)].x;
@@ -550,7 +566,7 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
                     float2 xa, xb;
                     real_split(za, zb, w, xa, xb);
                     int ia = spec_index<LR>(ca, ka), ib = spec_index<LR>(cb, kb);
-                    if (SEED) {
+                    if (sd) {
                         tspec[ia] = cscale(xa, sc);
                         tspec[ib] = cscale(xb, sc);
                     } else {
@@ -562,7 +578,7 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
                 }
             }
             __syncthreads();
-            if (pp == 0 && !SEED) {
+            if (pp == 0 && !sd) {
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     int seq, j;
@@ -583,16 +599,27 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
             const float2* sb = sbase + (2 * pp + 1) * 16 * LR + jj;
             float2* da = tspec + (2 * pp) * 16 * LR + jj;
             float2* db = tspec + (2 * pp + 1) * 16 * LR + jj;
+            if (sd) {
 #pragma unroll
-            for (int r = 0; r < 16; ++r) {
-                // W_32^r = e^{-i pi r/16} = (cos, -sin)(2 pi r/32), r < 16
-                const float2 w = r ? cmul(base, make_float2(w32(r).x, -w32(r).y)) : base;
-                float2 xa, xb;
-                real_split(x[r], x[16 + 15 - r], w, xa, xb);
-                if (SEED) {
-                    __stcs(da + r * LR, cscale(xa, sc));
-                    __stcs(db + (15 - r) * LR, cscale(xb, sc));
-                } else {
+                for (int r = 0; r < 16; ++r) {
+                    // W_32^r = e^{-i pi r/16} = (cos, -sin)(2 pi r/32), r < 16
+                    const float2 w = r ? cmul(base, make_float2(w32(r).x, -w32(r).y)) : base;
+                    float2 xa, xb;
+                    real_split(x[r], x[16 + 15 - r], w, xa, xb);
+                    if (FUSED) {  // parked for this CTA's key pass: keep it in L2
+                        da[r * LR] = cscale(xa, sc);
+                        db[(15 - r) * LR] = cscale(xb, sc);
+                    } else {
+                        __stcs(da + r * LR, cscale(xa, sc));
+                        __stcs(db + (15 - r) * LR, cscale(xb, sc));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < 16; ++r) {
+                    const float2 w = r ? cmul(base, make_float2(w32(r).x, -w32(r).y)) : base;
+                    float2 xa, xb;
+                    real_split(x[r], x[16 + 15 - r], w, xa, xb);
                     float2 qa, qb;
                     float2 fa, fb;
                     if (spec_smem) {
@@ -608,7 +635,12 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
                 }
             }
         }
-        if (SEED) continue;
+        if (sd) {
+            // the key pass copies the parked spectrum with the bulk-copy (async) proxy: order this
+            // thread's generic writes before it (the block barriers in between order the threads)
+            if (FUSED) fence_proxy_async_global();
+            continue;
+        }
 
         // ---- inverse column FFTs (radices 16, RB, RA) with the inverse 4-step twiddle folded into
         // the last stage: conj(W_N^{m1 k2}), m1 = j + NSL r
@@ -627,8 +659,8 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
         if (DIRECT) {  // after the last exchange sm is free until the next tile: the rest of its boxes
             __syncthreads();
             fence_proxy_async();
-            if (TMA) load_boxes(unit + (int)stride, early, NBOX, &bar);
-            else load_tile(unit + (int)stride);
+            if (TMA) load_boxes(next_u(), early, NBOX, &bar, map_next());
+            else load_tile(next_u(), map_next());
         }
 #pragma unroll
         for (int q = 0; q < QL; ++q) {
@@ -664,7 +696,8 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
             float2 a = sm[(2 * cp) * SP + padk<4>(m1)], b = sm[(2 * cp + 1) * SP + padk<4>(m1)];
             __stcg(Z4 + idx, make_float4(a.x, a.y, b.x, b.y));
         }
-    }
+    }  // part
+    }  // unit
     // every wait is behind: the barriers may be initialised again by a later call in the same CTA
     __syncthreads();
     if (t == 0) {

@@ -304,16 +304,24 @@ static int pass_a_l(const BlockGeom& g, const uint32_t* rows, bool seed, float2*
     return (int)cudaGetLastError();
 }
 
+// Pass B's shared memory without the early boxes: tile / exchange buffer, column tables, stage bases, and
+// the alignment of the TMA destination.
 template <int LOGL>
-static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y, float2* Z, float2* spec,
-                    int* err, int num_sms, cudaStream_t s, const Group& gp) {
+static constexpr size_t pass_b_smem() {
     constexpr int L = 1 << LOGL, CPT = 8192 / L, RL = Plan<LOGL>::RA, NSL = L / RL;
     constexpr bool LEAN = LOGL <= 6;
     constexpr int U1N = LEAN ? 0 : (NSL < 16 ? NSL : 16), U2N = LEAN ? 0 : NSL / U1N;
     constexpr size_t words = (size_t)CPT * TileStride<L>::value + (size_t)CPT * (RL + U1N + U2N) +
                              (size_t)PassBBases<LOGL, 256>::SLOTS * 256;
     static_assert(words * sizeof(float2) + 128 <= 112 * 1024, "pass B tile too large for two CTAs per SM");
-    const size_t smem = words * sizeof(float2) + 128;  // + alignment of the TMA destination
+    return words * sizeof(float2) + 128;
+}
+
+template <int LOGL>
+static int pass_b_l(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y, float2* Z, float2* spec,
+                    int* err, int num_sms, cudaStream_t s, const Group& gp) {
+    constexpr int L = 1 << LOGL, CPT = 8192 / L;
+    const size_t smem = pass_b_smem<LOGL>();
     // a group's CTAs walk all its blocks' tiles (one dimension); one block's walk its own
     const dim3 grid(grid_units(((1u << g.log_n2) / CPT) * gp.count, 2 * num_sms));
     // As many of the next tile's boxes as fit beside the tile while two CTAs stay resident per SM.
@@ -450,6 +458,27 @@ int launch_pass_b(const BlockGeom& g, bool seed, const PassMaps& maps, float2* Y
 #define C(LG) pass_b_l<LG>(g, seed, maps, Y, Z, spec, err, num_sms, s, gp)
     PA_COLS_DISPATCH(g.log_n1, C)
 #undef C
+}
+
+template <int LOGL>
+static int pass_b_fused_l(const BlockGeom& g, const PassMaps& seed_maps, const PassMaps& maps, float2* Z,
+                          float2* park, uint32_t park_ctas, int* err, int num_sms, cudaStream_t s) {
+    constexpr int L = 1 << LOGL, CPT = 8192 / L, BOXR = L < 256 ? L : 256;
+    static_assert(CPT * L * sizeof(float2) == kParkBytes, "a parked spectrum tile is one pass B tile");
+    const int grid = std::min(grid_units((1u << g.log_n2) / CPT, 2 * num_sms), (int)park_ctas);
+    if (grid < 1) return (int)cudaErrorInvalidValue;
+    return launch_pass_b_fused_k<LOGL>(dim3(grid), pass_b_smem<LOGL>(), (size_t)BOXR * CPT * sizeof(float2),
+                                       L / BOXR, seed_maps.y, maps.y, Z, g, park, err, s);
+}
+
+int launch_pass_b_fused(const BlockGeom& g, const PassMaps& seed_maps, const PassMaps& maps, float2* Z, float2* park,
+                        uint32_t park_ctas, int* err, int num_sms, cudaStream_t s) {
+    switch (g.log_n1) {
+        case 10: return pass_b_fused_l<10>(g, seed_maps, maps, Z, park, park_ctas, err, num_sms, s);
+        case 11: return pass_b_fused_l<11>(g, seed_maps, maps, Z, park, park_ctas, err, num_sms, s);
+        case 12: return pass_b_fused_l<12>(g, seed_maps, maps, Z, park, park_ctas, err, num_sms, s);
+        default: return (int)cudaErrorInvalidValue;
+    }
 }
 
 int launch_pass_c(const BlockGeom& g, const PassMaps& maps, const float2* Z, const unsigned long long* cnt,
