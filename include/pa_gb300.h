@@ -108,7 +108,8 @@ PA_API int pa_key_split(const uint32_t* recv_key, uint32_t n, uint32_t v, uint32
 /* Output length in bytes (PrivacyAmplification.cu:1197). */
 PA_API size_t pa_output_bytes(uint32_t n, uint32_t v, uint32_t flags);
 
-/* Number of kernels one pa_process_device launches for (n, v). */
+/* Number of kernels one pa_process_device launches for (n, v) with a cached seed spectrum (a one-use
+ * seed of 2^21 bits and more adds its two row-pass kernels: bit rows and row FFTs). */
 PA_API int pa_kernels_per_block(uint32_t n, uint32_t v, uint32_t flags);
 
 /* Per-kernel timing, the counterpart of the reference's STOPWATCH stage deltas
