@@ -415,288 +415,288 @@ __device__ __forceinline__ void pass_b_tiles(const CUtensorMap* mapY, const floa
     load_tile((int)first, FUSED ? mapYs : mapY);
     for (int unit = (int)first; unit < nunits; unit += (int)stride) {
 #pragma unroll
-    for (int part = 0; part < (FUSED ? 2 : 1); ++part) {
-        // sd: this part is a seed pass (FUSED: part 0 the seed's tile, part 1 the key's)
-        const bool sd = FUSED ? part == 0 : SEED;
-        const CUtensorMap* const map_self = FUSED && sd ? mapYs : mapY;
-        // the part after this one: FUSED alternates seed and key tiles, otherwise the next tile (formed
-        // where it is used, so that nothing extra stays live across the transform)
-        auto next_u = [&]() { return FUSED && sd ? unit : unit + (int)stride; };
-        auto map_next = [&]() { return FUSED ? (sd ? mapY : mapYs) : mapY; };
-        const int tile = unit_tile(unit);
-        const uint32_t blk = unit_block(unit);
-        // this block's spectrum: the seed pass writes it, the key pass reads it
-        float2* const bspec = !GRP ? spec : (SEED ? spec + ((size_t)blk << g.log_n) : const_cast<float2*>(ge[blk].spec));
-        // the tile's seed spectrum (contiguous) is read after the forward FFT: start it into L2 now
-        if (!FUSED && !SEED && t == 0)
-            prefetch_l2(bspec + (size_t)tile * (CPT * L), CPT * L * sizeof(float2));
-        // The rest of a part's boxes were issued by the part before it when that was a DIRECT key pass
-        // (after its last exchange); otherwise here, once every thread is done with sm.
-        const bool preloaded = DIRECT && (FUSED ? sd : !SEED);
-        const bool first_part = unit == (int)first && (!FUSED || sd);
-        if (!preloaded && !first_part) {
-            __syncthreads();  // previous tile done with sm
-            fence_proxy_async();
-            if (TMA) load_boxes(unit, early, NBOX, &bar, map_self);  // its first boxes came early
-            else load_tile(unit, map_self);
-        }
-        wait_tile();
-        __syncthreads();  // tile copies visible; previous tile done with the tables
-        // The tile's column tables are first read by the last inverse stage, several block barriers
-        // later: no barrier of their own, so the few threads computing them overlap the first stages.
-        if (!sd) {
-            for (int i = t; i < CPT * (RL + U1N + U2N); i += NT) {
-                int c, kind, r;
-                if (i < CPT * RL) { c = i / RL; r = i % RL; kind = 0; }
-                else if (i < CPT * (RL + U1N)) { c = (i - CPT * RL) / U1D; r = (i - CPT * RL) % U1D; kind = 1; }
-                else { c = (i - CPT * (RL + U1N)) / U2D; r = (i - CPT * (RL + U1N)) % U2D; kind = 2; }
-                uint64_t k2 = col_k2((uint32_t)tile * (CPT / 2) + (uint32_t)(c >> 1), c & 1, n2);
-                uint64_t mult = kind == 0 ? (uint64_t)NSL * r : (kind == 1 ? (uint64_t)r : (uint64_t)U1N * r);
-                uint64_t e = (mult * k2) & ((1ull << g.log_n) - 1);
-                float2 w = expmi_pi((uint32_t)(2 * e), g.log_n);
-                if (kind == 0) sigma[c * RL + r] = cconj(w);
-                else if (kind == 1) u1[c * U1N + r] = w;
-                else u2[c * U2N + r] = w;
-            }
-        }
-        float2 x[E];
-        if (TMA) {  // row-major tile: element m1 of column c at sm[m1 * CPT + c]
-#pragma unroll
-            for (int q = 0; q < E / P::RA; ++q) {
-                int seq, j;
-                Lin::template at<L, P::RA>(q, seq, j);
-#pragma unroll
-                for (int r = 0; r < P::RA; ++r) x[q * P::RA + r] = srow[(j + r * (L / P::RA)) * CPT + seq];
-            }
-        } else {
-            gather_inputs<L, SP, E, P::RA, Lin>(x, sm);
-        }
-        stage<P::RA, 1, -1, E>(x, nullptr);
-        // after the first exchange's barrier every thread has read the tile: the next tile's own boxes
-        // are copied under the rest of this tile's work
-        auto copy_early = [&]() {
-            if (early > 0) {
+        for (int part = 0; part < (FUSED ? 2 : 1); ++part) {
+            // sd: this part is a seed pass (FUSED: part 0 the seed's tile, part 1 the key's)
+            const bool sd = FUSED ? part == 0 : SEED;
+            const CUtensorMap* const map_self = FUSED && sd ? mapYs : mapY;
+            // the part after this one: FUSED alternates seed and key tiles, otherwise the next tile (formed
+            // where it is used, so that nothing extra stays live across the transform)
+            auto next_u = [&]() { return FUSED && sd ? unit : unit + (int)stride; };
+            auto map_next = [&]() { return FUSED ? (sd ? mapY : mapYs) : mapY; };
+            const int tile = unit_tile(unit);
+            const uint32_t blk = unit_block(unit);
+            // this block's spectrum: the seed pass writes it, the key pass reads it
+            float2* const bspec = !GRP ? spec : (SEED ? spec + ((size_t)blk << g.log_n) : const_cast<float2*>(ge[blk].spec));
+            // the tile's seed spectrum (contiguous) is read after the forward FFT: start it into L2 now
+            if (!FUSED && !SEED && t == 0)
+                prefetch_l2(bspec + (size_t)tile * (CPT * L), CPT * L * sizeof(float2));
+            // The rest of a part's boxes were issued by the part before it when that was a DIRECT key pass
+            // (after its last exchange); otherwise here, once every thread is done with sm.
+            const bool preloaded = DIRECT && (FUSED ? sd : !SEED);
+            const bool first_part = unit == (int)first && (!FUSED || sd);
+            if (!preloaded && !first_part) {
+                __syncthreads();  // previous tile done with sm
                 fence_proxy_async();
-                load_boxes(next_u(), 0, early, &bar_early, map_next());
+                if (TMA) load_boxes(unit, early, NBOX, &bar, map_self);  // its first boxes came early
+                else load_tile(unit, map_self);
             }
-        };
-        if (P::NSTAGE == 2) {
-            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm, copy_early);
-            float2 w[QB > 0 ? QB : 1];
+            wait_tile();
+            __syncthreads();  // tile copies visible; previous tile done with the tables
+            // The tile's column tables are first read by the last inverse stage, several block barriers
+            // later: no barrier of their own, so the few threads computing them overlap the first stages.
+            if (!sd) {
+                for (int i = t; i < CPT * (RL + U1N + U2N); i += NT) {
+                    int c, kind, r;
+                    if (i < CPT * RL) { c = i / RL; r = i % RL; kind = 0; }
+                    else if (i < CPT * (RL + U1N)) { c = (i - CPT * RL) / U1D; r = (i - CPT * RL) % U1D; kind = 1; }
+                    else { c = (i - CPT * (RL + U1N)) / U2D; r = (i - CPT * (RL + U1N)) % U2D; kind = 2; }
+                    uint64_t k2 = col_k2((uint32_t)tile * (CPT / 2) + (uint32_t)(c >> 1), c & 1, n2);
+                    uint64_t mult = kind == 0 ? (uint64_t)NSL * r : (kind == 1 ? (uint64_t)r : (uint64_t)U1N * r);
+                    uint64_t e = (mult * k2) & ((1ull << g.log_n) - 1);
+                    float2 w = expmi_pi((uint32_t)(2 * e), g.log_n);
+                    if (kind == 0) sigma[c * RL + r] = cconj(w);
+                    else if (kind == 1) u1[c * U1N + r] = w;
+                    else u2[c * U2N + r] = w;
+                }
+            }
+            float2 x[E];
+            if (TMA) {  // row-major tile: element m1 of column c at sm[m1 * CPT + c]
 #pragma unroll
-            for (int q = 0; q < QB; ++q) w[q] = tws[TB::f2(q) * NT + t];
-            stage<P::RB, P::RA, -1, E>(x, w);
-            exchange<L, SP, 4, E, P::RB, P::RA, Lin, 16, MapMirrorPair>(x, sm);
-        } else {
-            exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorPair>(x, sm, copy_early);
-        }
-        float2* tspec = FUSED ? spec + (size_t)first * (CPT * L) : bspec + (size_t)tile * (CPT * L);
-        const bool special = tile == 0;  // pair 0 holds the self-mirrored columns 0 and N2/2
-        // Key pass: the tile buffer is free until the inverse exchange, so the tile's seed spectrum
-        // (CPT * L values, contiguous) is copied into it while the mirror stage computes, and the
-        // spectral step reads shared memory instead of waiting on L2.
-        const bool spec_smem = !sd && !special;
-        if (spec_smem) {
-            __syncthreads();  // every thread done reading sm
-            fence_proxy_async();
-            constexpr uint32_t kBytes = CPT * L * sizeof(float2), kChunk = 16384;
-            if (t == 0) mbar_expect_tx(&bar_spec, kBytes);
-            if ((t & 31) == 0) {  // one chunk per warp
+                for (int q = 0; q < E / P::RA; ++q) {
+                    int seq, j;
+                    Lin::template at<L, P::RA>(q, seq, j);
+#pragma unroll
+                    for (int r = 0; r < P::RA; ++r) x[q * P::RA + r] = srow[(j + r * (L / P::RA)) * CPT + seq];
+                }
+            } else {
+                gather_inputs<L, SP, E, P::RA, Lin>(x, sm);
+            }
+            stage<P::RA, 1, -1, E>(x, nullptr);
+            // after the first exchange's barrier every thread has read the tile: the next tile's own boxes
+            // are copied under the rest of this tile's work
+            auto copy_early = [&]() {
+                if (early > 0) {
+                    fence_proxy_async();
+                    load_boxes(next_u(), 0, early, &bar_early, map_next());
+                }
+            };
+            if (P::NSTAGE == 2) {
+                exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, P::RB, Lin>(x, sm, copy_early);
+                float2 w[QB > 0 ? QB : 1];
+#pragma unroll
+                for (int q = 0; q < QB; ++q) w[q] = tws[TB::f2(q) * NT + t];
+                stage<P::RB, P::RA, -1, E>(x, w);
+                exchange<L, SP, 4, E, P::RB, P::RA, Lin, 16, MapMirrorPair>(x, sm);
+            } else {
+                exchange<L, SP, PadAfterFirst<P::RA>::value, E, P::RA, 1, Lin, 16, MapMirrorPair>(x, sm, copy_early);
+            }
+            float2* tspec = FUSED ? spec + (size_t)first * (CPT * L) : bspec + (size_t)tile * (CPT * L);
+            const bool special = tile == 0;  // pair 0 holds the self-mirrored columns 0 and N2/2
+            // Key pass: the tile buffer is free until the inverse exchange, so the tile's seed spectrum
+            // (CPT * L values, contiguous) is copied into it while the mirror stage computes, and the
+            // spectral step reads shared memory instead of waiting on L2.
+            const bool spec_smem = !sd && !special;
+            if (spec_smem) {
+                __syncthreads();  // every thread done reading sm
+                fence_proxy_async();
+                constexpr uint32_t kBytes = CPT * L * sizeof(float2), kChunk = 16384;
+                if (t == 0) mbar_expect_tx(&bar_spec, kBytes);
+                if ((t & 31) == 0) {  // one chunk per warp
 #pragma unroll 1
-                for (uint32_t off = (uint32_t)(t >> 5) * kChunk; off < kBytes; off += (NT / 32) * kChunk)
-                    bulk_load(reinterpret_cast<char*>(sm) + off, reinterpret_cast<const char*>(tspec) + off, kChunk,
-                              &bar_spec);
-            }
-        }
-        {
-            float2 w[2] = {tws[TB::M * NT + t], tws[(TB::M + 1) * NT + t]};
-            stage<16, LR, -1, E>(x, w);
-        }
-        if (spec_smem) {
-            if (!s_fail && !mbar_wait(&bar_spec, parity_spec)) {
-                s_fail = 1;
-                atomicExch(err, kErrTmaTimeout);
-            }
-            parity_spec ^= 1u;
-        }
-
-        // ---- spectral step: real split, product with the seed spectrum, real merge
-        if (special) {
-            __syncthreads();
-            if (pp == 0) {
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    int seq, j;
-                    MapMirrorPair::at<L, 16>(q, seq, j);
-                    float2* b = sm + seq * SP + padk<4>(j);
-#pragma unroll
-                    for (int r = 0; r < 16; ++r) b[padoff<4>(LR * r)] = x[16 * q + r];
+                    for (uint32_t off = (uint32_t)(t >> 5) * kChunk; off < kBytes; off += (NT / 32) * kChunk)
+                        bulk_load(reinterpret_cast<char*>(sm) + off, reinterpret_cast<const char*>(tspec) + off, kChunk,
+                                  &bar_spec);
                 }
             }
-            __syncthreads();
-            if (pp == 0) {
-                for (int u = jj; u < L; u += LR) {
-                    int ca, ka, cb, kb;
-                    uint32_t k;
-                    if (u < L / 2) {  // column k2 = 0, rows u <-> L-u
-                        ca = cb = 0;
-                        ka = u;
-                        kb = u ? L - u : L / 2;
-                        k = n2 * (uint32_t)ka;
-                    } else {  // column k2 = N2/2, rows j <-> L-1-j
-                        ca = cb = 1;
-                        ka = u - L / 2;
-                        kb = L - 1 - ka;
-                        k = n2 / 2 + n2 * (uint32_t)ka;
+            {
+                float2 w[2] = {tws[TB::M * NT + t], tws[(TB::M + 1) * NT + t]};
+                stage<16, LR, -1, E>(x, w);
+            }
+            if (spec_smem) {
+                if (!s_fail && !mbar_wait(&bar_spec, parity_spec)) {
+                    s_fail = 1;
+                    atomicExch(err, kErrTmaTimeout);
+                }
+                parity_spec ^= 1u;
+            }
+
+            // ---- spectral step: real split, product with the seed spectrum, real merge
+            if (special) {
+                __syncthreads();
+                if (pp == 0) {
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        int seq, j;
+                        MapMirrorPair::at<L, 16>(q, seq, j);
+                        float2* b = sm + seq * SP + padk<4>(j);
+#pragma unroll
+                        for (int r = 0; r < 16; ++r) b[padoff<4>(LR * r)] = x[16 * q + r];
                     }
-                    if (u == 0) {  // DC (dropped) and Nyquist in slot (0, 0); then the self pair N/2
-                        float2 z = sm[padk<4>(0)];
-                        float nyq = 2.0f * (z.x - z.y);
-                        if (sd) {
-                            tspec[spec_index<LR>(0, 0)] = make_float2(nyq * sc, 0.f);
-                        } else {
-                            float pn = nyq * tspec[spec_index<LR>(0, 0)].x;
-                            sm[padk<4>(0)] = make_float2(pn, -pn);
+                }
+                __syncthreads();
+                if (pp == 0) {
+                    for (int u = jj; u < L; u += LR) {
+                        int ca, ka, cb, kb;
+                        uint32_t k;
+                        if (u < L / 2) {  // column k2 = 0, rows u <-> L-u
+                            ca = cb = 0;
+                            ka = u;
+                            kb = u ? L - u : L / 2;
+                            k = n2 * (uint32_t)ka;
+                        } else {  // column k2 = N2/2, rows j <-> L-1-j
+                            ca = cb = 1;
+                            ka = u - L / 2;
+                            kb = L - 1 - ka;
+                            k = n2 / 2 + n2 * (uint32_t)ka;
                         }
-                        ka = kb = L / 2;
-                        k = n2 * (uint32_t)(L / 2);
+                        if (u == 0) {  // DC (dropped) and Nyquist in slot (0, 0); then the self pair N/2
+                            float2 z = sm[padk<4>(0)];
+                            float nyq = 2.0f * (z.x - z.y);
+                            if (sd) {
+                                tspec[spec_index<LR>(0, 0)] = make_float2(nyq * sc, 0.f);
+                            } else {
+                                float pn = nyq * tspec[spec_index<LR>(0, 0)].x;
+                                sm[padk<4>(0)] = make_float2(pn, -pn);
+                            }
+                            ka = kb = L / 2;
+                            k = n2 * (uint32_t)(L / 2);
+                        }
+                        float2 w = expmi_pi(k, g.log_n);
+                        float2 za = sm[ca * SP + padk<4>(ka)], zb = sm[cb * SP + padk<4>(kb)];
+                        float2 xa, xb;
+                        real_split(za, zb, w, xa, xb);
+                        int ia = spec_index<LR>(ca, ka), ib = spec_index<LR>(cb, kb);
+                        if (sd) {
+                            tspec[ia] = cscale(xa, sc);
+                            tspec[ib] = cscale(xb, sc);
+                        } else {
+                            float2 qa, qb;
+                            real_merge(cmul(xa, tspec[ia]), cmul(xb, tspec[ib]), w, qa, qb);
+                            sm[ca * SP + padk<4>(ka)] = qa;
+                            sm[cb * SP + padk<4>(kb)] = qb;
+                        }
                     }
-                    float2 w = expmi_pi(k, g.log_n);
-                    float2 za = sm[ca * SP + padk<4>(ka)], zb = sm[cb * SP + padk<4>(kb)];
-                    float2 xa, xb;
-                    real_split(za, zb, w, xa, xb);
-                    int ia = spec_index<LR>(ca, ka), ib = spec_index<LR>(cb, kb);
-                    if (sd) {
-                        tspec[ia] = cscale(xa, sc);
-                        tspec[ib] = cscale(xb, sc);
-                    } else {
+                }
+                __syncthreads();
+                if (pp == 0 && !sd) {
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        int seq, j;
+                        MapMirrorPair::at<L, 16>(q, seq, j);
+                        const float2* b = sm + seq * SP + padk<4>(j);
+#pragma unroll
+                        for (int r = 0; r < 16; ++r) x[16 * q + r] = b[padoff<4>(LR * r)];
+                    }
+                }
+            }
+            if (!special || pp != 0) {
+                // bins (k1 = jj + LR r, k2 = p) and (L-1-k1, N2-p): x[r] and x[16 + 15 - r];
+                // W_2N^{p + N2 (jj + LR r)} = W_2N^{p + N2 jj} * W_32^r
+                const uint32_t p = (uint32_t)tile * (CPT / 2) + (uint32_t)pp;
+                const float2 base = expmi_pi(p + n2 * (uint32_t)jj, g.log_n);
+                const float2* sbase = spec_smem ? sm : tspec;  // key pass: the copy in shared memory
+                const float2* sa = sbase + (2 * pp) * 16 * LR + jj;
+                const float2* sb = sbase + (2 * pp + 1) * 16 * LR + jj;
+                float2* da = tspec + (2 * pp) * 16 * LR + jj;
+                float2* db = tspec + (2 * pp + 1) * 16 * LR + jj;
+                if (sd) {
+#pragma unroll
+                    for (int r = 0; r < 16; ++r) {
+                        // W_32^r = e^{-i pi r/16} = (cos, -sin)(2 pi r/32), r < 16
+                        const float2 w = r ? cmul(base, make_float2(w32(r).x, -w32(r).y)) : base;
+                        float2 xa, xb;
+                        real_split(x[r], x[16 + 15 - r], w, xa, xb);
+                        if (FUSED) {  // parked for this CTA's key pass: keep it in L2
+                            da[r * LR] = cscale(xa, sc);
+                            db[(15 - r) * LR] = cscale(xb, sc);
+                        } else {
+                            __stcs(da + r * LR, cscale(xa, sc));
+                            __stcs(db + (15 - r) * LR, cscale(xb, sc));
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int r = 0; r < 16; ++r) {
+                        const float2 w = r ? cmul(base, make_float2(w32(r).x, -w32(r).y)) : base;
+                        float2 xa, xb;
+                        real_split(x[r], x[16 + 15 - r], w, xa, xb);
                         float2 qa, qb;
-                        real_merge(cmul(xa, tspec[ia]), cmul(xb, tspec[ib]), w, qa, qb);
-                        sm[ca * SP + padk<4>(ka)] = qa;
-                        sm[cb * SP + padk<4>(kb)] = qb;
+                        float2 fa, fb;
+                        if (spec_smem) {
+                            fa = sa[r * LR];
+                            fb = sb[(15 - r) * LR];
+                        } else {
+                            fa = __ldcs(sa + r * LR);
+                            fb = __ldcs(sb + (15 - r) * LR);
+                        }
+                        real_merge(cmul(xa, fa), cmul(xb, fb), w, qa, qb);
+                        x[r] = qa;
+                        x[16 + 15 - r] = qb;
                     }
                 }
             }
-            __syncthreads();
-            if (pp == 0 && !sd) {
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    int seq, j;
-                    MapMirrorPair::at<L, 16>(q, seq, j);
-                    const float2* b = sm + seq * SP + padk<4>(j);
-#pragma unroll
-                    for (int r = 0; r < 16; ++r) x[16 * q + r] = b[padoff<4>(LR * r)];
-                }
-            }
-        }
-        if (!special || pp != 0) {
-            // bins (k1 = jj + LR r, k2 = p) and (L-1-k1, N2-p): x[r] and x[16 + 15 - r];
-            // W_2N^{p + N2 (jj + LR r)} = W_2N^{p + N2 jj} * W_32^r
-            const uint32_t p = (uint32_t)tile * (CPT / 2) + (uint32_t)pp;
-            const float2 base = expmi_pi(p + n2 * (uint32_t)jj, g.log_n);
-            const float2* sbase = spec_smem ? sm : tspec;  // key pass: the copy in shared memory
-            const float2* sa = sbase + (2 * pp) * 16 * LR + jj;
-            const float2* sb = sbase + (2 * pp + 1) * 16 * LR + jj;
-            float2* da = tspec + (2 * pp) * 16 * LR + jj;
-            float2* db = tspec + (2 * pp + 1) * 16 * LR + jj;
             if (sd) {
-#pragma unroll
-                for (int r = 0; r < 16; ++r) {
-                    // W_32^r = e^{-i pi r/16} = (cos, -sin)(2 pi r/32), r < 16
-                    const float2 w = r ? cmul(base, make_float2(w32(r).x, -w32(r).y)) : base;
-                    float2 xa, xb;
-                    real_split(x[r], x[16 + 15 - r], w, xa, xb);
-                    if (FUSED) {  // parked for this CTA's key pass: keep it in L2
-                        da[r * LR] = cscale(xa, sc);
-                        db[(15 - r) * LR] = cscale(xb, sc);
-                    } else {
-                        __stcs(da + r * LR, cscale(xa, sc));
-                        __stcs(db + (15 - r) * LR, cscale(xb, sc));
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int r = 0; r < 16; ++r) {
-                    const float2 w = r ? cmul(base, make_float2(w32(r).x, -w32(r).y)) : base;
-                    float2 xa, xb;
-                    real_split(x[r], x[16 + 15 - r], w, xa, xb);
-                    float2 qa, qb;
-                    float2 fa, fb;
-                    if (spec_smem) {
-                        fa = sa[r * LR];
-                        fb = sb[(15 - r) * LR];
-                    } else {
-                        fa = __ldcs(sa + r * LR);
-                        fb = __ldcs(sb + (15 - r) * LR);
-                    }
-                    real_merge(cmul(xa, fa), cmul(xb, fb), w, qa, qb);
-                    x[r] = qa;
-                    x[16 + 15 - r] = qb;
-                }
+                // the key pass copies the parked spectrum with the bulk-copy (async) proxy: order this
+                // thread's generic writes before it (the block barriers in between order the threads)
+                if (FUSED) fence_proxy_async_global();
+                continue;
             }
-        }
-        if (sd) {
-            // the key pass copies the parked spectrum with the bulk-copy (async) proxy: order this
-            // thread's generic writes before it (the block barriers in between order the threads)
-            if (FUSED) fence_proxy_async_global();
-            continue;
-        }
 
-        // ---- inverse column FFTs (radices 16, RB, RA) with the inverse 4-step twiddle folded into
-        // the last stage: conj(W_N^{m1 k2}), m1 = j + NSL r
-        stage<16, 1, +1, E>(x, nullptr);
-        if (P::NSTAGE == 2) {
-            exchange<L, SP, 4, E, 16, 1, MapMirrorPair, P::RB, Lin>(x, sm);
-            float2 w[QB > 0 ? QB : 1];
+            // ---- inverse column FFTs (radices 16, RB, RA) with the inverse 4-step twiddle folded into
+            // the last stage: conj(W_N^{m1 k2}), m1 = j + NSL r
+            stage<16, 1, +1, E>(x, nullptr);
+            if (P::NSTAGE == 2) {
+                exchange<L, SP, 4, E, 16, 1, MapMirrorPair, P::RB, Lin>(x, sm);
+                float2 w[QB > 0 ? QB : 1];
 #pragma unroll
-            for (int q = 0; q < QB; ++q)
-                w[q] = TB::SHARE2 ? cconj(tws[TB::f2(q) * NT + t]) : tws[TB::i2(q) * NT + t];
-            stage<P::RB, 16, +1, E>(x, w);
-            exchange<L, SP, 4, E, P::RB, 16, Lin, RL, Lin>(x, sm);
-        } else {
-            exchange<L, SP, 4, E, 16, 1, MapMirrorPair, RL, Lin>(x, sm);
-        }
-        if (DIRECT) {  // after the last exchange sm is free until the next tile: the rest of its boxes
-            __syncthreads();
-            fence_proxy_async();
-            if (TMA) load_boxes(next_u(), early, NBOX, &bar, map_next());
-            else load_tile(next_u(), map_next());
-        }
-#pragma unroll
-        for (int q = 0; q < QL; ++q) {
-            int seq, j;
-            Lin::template at<L, RL>(q, seq, j);
-            float2 c, wbase;
-            if (LEAN) {
-                uint32_t k2 = col_k2((uint32_t)tile * (CPT / 2) + (uint32_t)(seq >> 1), seq & 1, n2);
-                c = cconj(expmi_pi((uint32_t)((2ull * j * k2) & ((2ull << g.log_n) - 1)), g.log_n));
-                wbase = unit_root<+1>(j % NSL, NSL * RL);
+                for (int q = 0; q < QB; ++q)
+                    w[q] = TB::SHARE2 ? cconj(tws[TB::f2(q) * NT + t]) : tws[TB::i2(q) * NT + t];
+                stage<P::RB, 16, +1, E>(x, w);
+                exchange<L, SP, 4, E, P::RB, 16, Lin, RL, Lin>(x, sm);
             } else {
-                c = cconj(cmul(u1[seq * U1N + j % U1D], u2[seq * U2N + j / U1D]));
-                wbase = tws[TB::ls(q) * NT + t];
+                exchange<L, SP, 4, E, 16, 1, MapMirrorPair, RL, Lin>(x, sm);
             }
-            twiddle_powers<RL, true>(&x[q * RL], wbase, c);
-            dft<RL, +1>(reinterpret_cast<float2(&)[RL]>(x[q * RL]));
+            if (DIRECT) {  // after the last exchange sm is free until the next tile: the rest of its boxes
+                __syncthreads();
+                fence_proxy_async();
+                if (TMA) load_boxes(next_u(), early, NBOX, &bar, map_next());
+                else load_tile(next_u(), map_next());
+            }
 #pragma unroll
-            for (int r = 0; r < RL; ++r) x[q * RL + r] = cmul(x[q * RL + r], sigma[seq * RL + r]);
-        }
-        float4* Z4 = reinterpret_cast<float4*>(Z + ((size_t)blk << g.log_n)) + (size_t)tile * L * (CPT / 2);  // [m1][CPT/2]
-        if (DIRECT) {  // thread holds column 0 (x[0..RL)) and column 1 (x[RL..2RL)) of rows j + NSL r
+            for (int q = 0; q < QL; ++q) {
+                int seq, j;
+                Lin::template at<L, RL>(q, seq, j);
+                float2 c, wbase;
+                if (LEAN) {
+                    uint32_t k2 = col_k2((uint32_t)tile * (CPT / 2) + (uint32_t)(seq >> 1), seq & 1, n2);
+                    c = cconj(expmi_pi((uint32_t)((2ull * j * k2) & ((2ull << g.log_n) - 1)), g.log_n));
+                    wbase = unit_root<+1>(j % NSL, NSL * RL);
+                } else {
+                    c = cconj(cmul(u1[seq * U1N + j % U1D], u2[seq * U2N + j / U1D]));
+                    wbase = tws[TB::ls(q) * NT + t];
+                }
+                twiddle_powers<RL, true>(&x[q * RL], wbase, c);
+                dft<RL, +1>(reinterpret_cast<float2(&)[RL]>(x[q * RL]));
 #pragma unroll
-            for (int r = 0; r < RL; ++r)
-                __stcg(Z4 + t + NSL * r, make_float4(x[r].x, x[r].y, x[RL + r].x, x[RL + r].y));
-            continue;
-        }
-        __syncthreads();
-        scatter_outputs<L, SP, E, RL, Lin>(x, sm);
-        __syncthreads();
+                for (int r = 0; r < RL; ++r) x[q * RL + r] = cmul(x[q * RL + r], sigma[seq * RL + r]);
+            }
+            float4* Z4 = reinterpret_cast<float4*>(Z + ((size_t)blk << g.log_n)) + (size_t)tile * L * (CPT / 2);  // [m1][CPT/2]
+            if (DIRECT) {  // thread holds column 0 (x[0..RL)) and column 1 (x[RL..2RL)) of rows j + NSL r
+#pragma unroll
+                for (int r = 0; r < RL; ++r)
+                    __stcg(Z4 + t + NSL * r, make_float4(x[r].x, x[r].y, x[RL + r].x, x[RL + r].y));
+                continue;
+            }
+            __syncthreads();
+            scatter_outputs<L, SP, E, RL, Lin>(x, sm);
+            __syncthreads();
 #pragma unroll 4
-        for (int i = 0; i < L * CPT / 2 / NT; ++i) {
-            int idx = t + i * NT, m1 = idx / (CPT / 2), cp = idx % (CPT / 2);
-            float2 a = sm[(2 * cp) * SP + padk<4>(m1)], b = sm[(2 * cp + 1) * SP + padk<4>(m1)];
-            __stcg(Z4 + idx, make_float4(a.x, a.y, b.x, b.y));
-        }
-    }  // part
+            for (int i = 0; i < L * CPT / 2 / NT; ++i) {
+                int idx = t + i * NT, m1 = idx / (CPT / 2), cp = idx % (CPT / 2);
+                float2 a = sm[(2 * cp) * SP + padk<4>(m1)], b = sm[(2 * cp + 1) * SP + padk<4>(m1)];
+                __stcg(Z4 + idx, make_float4(a.x, a.y, b.x, b.y));
+            }
+        }  // part
     }  // unit
     // every wait is behind: the barriers may be initialised again by a later call in the same CTA
     __syncthreads();
