@@ -1,11 +1,12 @@
 """Runs a few device-resident blocks of one size back to back, for a profiler's launch list or capture.
 
     python -m privacyamplification_gb300.profile_block [--log-n 27] [--blocks 4] [--v-frac 0.375]
-                                                       [--lanes [--ctas-per-lane T]]
+                                                       [--lanes [--ctas-per-lane T]] [--one-use-seed]
 
 Seed and keys are i.i.d. Bernoulli(0.5) bits from fixed PCG64 seeds (the bench's inputs at n = 2^27); the
 seed spectrum is computed once, then `blocks` key blocks run through pa_process_device on one stream
-(or, with --lanes, as one persistent lane batch of that many blocks).  Prints the per-kernel mean device
+(or, with --lanes, as one persistent lane batch of that many blocks).  With --one-use-seed the seed is
+set again before every block for that block only, so each block transforms it in its own column pass.  Prints the per-kernel mean device
 times the engine records, so a profiled run can be matched with the unprofiled one.
 """
 from __future__ import annotations
@@ -22,6 +23,8 @@ def main():
     ap.add_argument("--lanes", action="store_true", help="run the blocks as one persistent lane batch")
     ap.add_argument("--ctas-per-lane", type=int, default=0, help="lane width (0: the engine's default)")
     ap.add_argument("--repeat", type=int, default=1, help="lane batches run (the last one is reported)")
+    ap.add_argument("--one-use-seed", action="store_true",
+                    help="set the seed before every block for that block only (the fused column pass)")
     args = ap.parse_args()
     import numpy as np
     import torch
@@ -50,10 +53,14 @@ def main():
             print(json.dumps({"n": n, "v": v, "blocks": args.blocks, "lanes": eng.set_lanes(0, 0),
                               "batch_ms": st[0].gpu_ms, "max_residual": max(s.max_residual for s in st)}))
             return
-        eng.set_seed(seed, n, -1)
         s = torch.cuda.Stream(device=dev)
+        d_seed = d(seed)
+        if not args.one_use_seed:
+            eng.set_seed(seed, n, -1)
         eng.set_timing(True)
         for i in range(args.blocks):
+            if args.one_use_seed:  # queued on the blocks' stream, after the previous block's reads
+                eng.set_seed_device(d_seed.data_ptr(), n, 1, stream=s.cuda_stream)
             ks, kr = d_keys[i % 2]
             eng.process_device(ks.data_ptr(), kr.data_ptr(), n, v, out.data_ptr(), stream=s.cuda_stream)
         st = eng.sync()
